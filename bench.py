@@ -1,0 +1,297 @@
+"""Benchmark of the SCFT propagator hot path on GB300.
+
+Metric: Gpt*step/s (grid points x contour steps per second) at 128^3, Ns=200,
+reported with the HBM-roofline fraction of the propagator march.
+
+One "step" = one SCF iteration of the reference's Free loop
+(cuda_scft.cu:167-186): average_value x3, four propagator marches
+(2*(NsA+dNsB) contour steps over M points), Q, phi and the field update.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N>1 runs under torchrun: every rank solves its own independent replica (the
+path has no exchange step), and rank 0 prints the whole-job rate computed
+from the max-over-ranks time.  --impl reference times the reference's
+algorithm on the host cores (the reference has no CPU path of its own, so
+this is the CPU restatement with threaded scipy.fft) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gpt·step/s at 128³ Ns=200 (%HBM roofline); s-to-converge vs plain FP64 GPU"
+UNIT = "Gpt*step/s"
+N, L, CHIN, FA, DS = 128, 3.8, 18.0, 0.36, 0.005
+WORKLOAD = ("128^3 periodic grid, double-gyroid init chiN*0.2*g(r)+N(0,0.02) seed 0, "
+            "f=0.36, chiN=18, box 3.8 Rg, Ns=200 (ds=0.005, NsA=72, dNsB=128), "
+            "1 SCF iteration (4 propagator marches + Q + phi + simple mixing) per step")
+BYTES_PER_PT_STEP = {"fp32": 12.0, "fp64": 24.0}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = None
+        try:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 8:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    smax.append(float(parts[1]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[4:8]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(seconds=12.0):
+    """The CPU restatement (scipy.fft, all host threads) on a bounded sample of
+    the same workload: forward split steps of one 128^3 propagator."""
+    from oracle import scft_oracle as orc
+    import __graft_entry__ as ge
+    ge.load_package()
+    from scft_gb300 import fields as fl
+    p = orc.Params(nx=N, ny=N, nz=N, lx=L, ly=L, lz=L, hAB=CHIN, fA=FA, ds0=DS)
+    wa, _ = fl.gyroid(N, N, N, L, L, L, CHIN, seed=0)
+    workers = os.cpu_count()
+    orc.march_rate_cpu(p, wa, 1, workers)   # warm-up (plans, pages)
+    done_s, done_pts, steps = 0.0, 0, 0
+    while done_s < seconds or steps < 3:
+        dt, pts = orc.march_rate_cpu(p, wa, 2, workers)
+        done_s += dt
+        done_pts += pts
+        steps += 2
+    return {"value": done_pts / done_s / 1e9, "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": f"{steps} forward split steps of one 128^3 propagator (scipy.fft pocketfft, "
+                      f"FP64, {workers} threads), {done_s:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import scft_oracle as orc
+    import __graft_entry__ as ge
+    ge.load_package()
+    from scft_gb300 import fields as fl
+    p = orc.Params(nx=N, ny=N, nz=N, lx=L, ly=L, lz=L, hAB=CHIN, fA=FA, ds0=DS)
+    wa, _ = fl.gyroid(N, N, N, L, L, L, CHIN, seed=0)
+    workers = os.cpu_count()
+    sample = 8   # split steps per bench step (a bounded sample of the march)
+    for _ in range(args.warmup):
+        orc.march_rate_cpu(p, wa, sample, workers)
+    tot, pts = 0.0, 0
+    for _ in range(args.steps):
+        dt, n = orc.march_rate_cpu(p, wa, sample, workers)
+        tot += dt
+        pts += n
+    value = pts / tot / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD + " (reference arm: 8 split steps of one propagator "
+                               "per step)", "grid": [N, N, N], "Ns": 200},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
+                         "sample": f"{sample} forward split steps of one 128^3 propagator per "
+                                   f"step; the reference has no CPU path (init.cpp:119-125), "
+                                   f"so its algorithm runs as the CPU restatement with "
+                                   f"scipy.fft on {workers} threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from scft_gb300 import fields as fl
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = local if ws > 1 else 0
+    prec = pkg.PREC_FP64 if args.precision == "fp64" else pkg.PREC_FP32
+    ctx = pkg.Context(nx=N, ny=N, nz=N, lx=L, ly=L, lz=L, hAB=CHIN, fA=FA, ds0=DS,
+                      precision=prec, device=dev)
+    wa, wb = fl.gyroid(N, N, N, L, L, L, CHIN, seed=rank)
+    ctx.set_w(wa, wb)
+    pt_steps = 2 * (ctx.NsA + ctx.dNsB) * N ** 3
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        ctx.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up
+    for _ in range(args.warmup):
+        ctx.iterate(1)
+    barrier()
+
+    # ---- timed region: K steps, device events on the library's stream
+    clocks = ClockSampler(dev) if rank == 0 else None
+    l0 = ctx.launch_count()
+    ctx.profile_enable(4 * args.steps + 8)
+    t0 = time.perf_counter()
+    ms = ctx.time_iterations(args.steps)
+    wall = time.perf_counter() - t0
+    march_ms, n_marches, march_pts = ctx.profile_read()
+    ctx.profile_enable(0)
+    launches = ctx.launch_count() - l0
+    barrier()
+    clk = clocks.stop() if clocks else None
+    t_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = ws * pt_steps * args.steps / (t_max / 1e3) / 1e9
+
+    # ---- end-to-end through the C ABI with pinned host buffers
+    hw_a = torch.from_numpy(wa.reshape(-1)).pin_memory()
+    hw_b = torch.from_numpy(wb.reshape(-1)).pin_memory()
+    ho_a = torch.empty(N ** 3, dtype=torch.float64).pin_memory()
+    ho_b = torch.empty(N ** 3, dtype=torch.float64).pin_memory()
+    import ctypes as C
+    dptr = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_double))
+    out5 = np.empty(5)
+    e2e_steps = max(1, min(args.steps, 5))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx._ck(ctx.lib.scft_set_field(ctx.h, pkg.FIELD_WA, dptr(hw_a)))
+        ctx._ck(ctx.lib.scft_set_field(ctx.h, pkg.FIELD_WB, dptr(hw_b)))
+        ctx._ck(ctx.lib.scft_iterate(ctx.h, 1, out5.ctypes.data_as(C.POINTER(C.c_double))))
+        ctx._ck(ctx.lib.scft_get_field(ctx.h, pkg.FIELD_PHA, dptr(ho_a)))
+        ctx._ck(ctx.lib.scft_get_field(ctx.h, pkg.FIELD_PHB, dptr(ho_b)))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = ws * pt_steps * e2e_steps / e2e_s / 1e9
+
+    if rank == 0:
+        peak, peak_kind = load_peaks()
+        bpp = BYTES_PER_PT_STEP[args.precision]
+        march_rate = march_pts / (march_ms / 1e3)          # pt-steps/s inside marches
+        achieved = march_rate * bpp / 1e9                  # GB/s, algorithmic bytes
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "fp32" else "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": [N, N, N], "Ns": 200, "batch": 1,
+                       "propagation": args.precision,
+                       "reductions": "fp64 (Q, F, mixing); phi contour sum compensated",
+                       "l2": "inputs larger than L2: each step streams 3.2 GB of propagator "
+                             "slices (fp32) through HBM",
+                       "parallelism": f"replicas x{ws} (no exchange step)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_kind": peak_kind,
+                         "kernel": "propagator march (sovDifFft): per-axis line-filter passes",
+                         "bytes_per_point_step": bpp,
+                         "march_ms_avg": march_ms / max(n_marches, 1),
+                         "marches_timed": n_marches},
+            "cpu_baseline": cpu_baseline() if not args.no_cpu else None,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * N ** 3,
+                    "d2h_bytes_per_step": 2 * 8 * N ** 3 + 5 * 8, "steps": e2e_steps},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "wall_s_timed": wall,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

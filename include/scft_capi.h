@@ -1,0 +1,192 @@
+/*
+ * scft_capi.h -- C ABI of the GB300-native diblock-copolymer SCFT hot path.
+ *
+ * One opaque context = one GPU, `batch` independent SCFT instances of one
+ * grid/parameter set (the reference's CUFFT_INFO + GPU_INFO, struct.h:19-125,
+ * with its GPU_N split collapsed to one device).  All entry points return an
+ * SCFT_* status code and never exit the process; scft_last_error() gives the
+ * message of the last failure on a context.
+ *
+ * Field arrays crossing this boundary are host float64 arrays laid out
+ * [batch][Nz][Ny][Nx] (x fastest), the reference's ijk order
+ * (init_cuda.cu:420-423, :509-512).  Propagators are stored on the device
+ * contour-outer ([batch][s][Nz][Ny][Nx]) in the context's propagation
+ * precision.
+ *
+ * Each declaration names the reference function it replaces (file:line).
+ */
+#ifndef SCFT_CAPI_H
+#define SCFT_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SCFT_OK 0
+#define SCFT_ERR_INVALID_ARG 1    /* bad pointer, size, enum or parameter */
+#define SCFT_ERR_UNSUPPORTED 2    /* grid the kernels do not handle (see scft_grid_supported) */
+#define SCFT_ERR_CUDA 3           /* CUDA runtime error (message in scft_last_error) */
+#define SCFT_ERR_NO_MEMORY 4      /* device or host allocation failed */
+#define SCFT_ERR_NOT_FINITE 5     /* NaN/Inf detected in Q, F or the residual */
+#define SCFT_ERR_IO 6             /* config / field file missing or malformed */
+#define SCFT_ERR_NO_DEVICE 7      /* no CUDA device / bad ordinal */
+
+/* ---- enums ---- */
+#define SCFT_PREC_FP64 0          /* plain path: propagation and FFTs in FP64 */
+#define SCFT_PREC_FP32 1          /* FP32 propagation, FP64 Q / contour sums / F / mixing */
+
+#define SCFT_FIELD_WA 0
+#define SCFT_FIELD_WB 1
+#define SCFT_FIELD_PHA 2
+#define SCFT_FIELD_PHB 3
+
+/* propagators, named after the reference's buffers (struct.h:118-121) */
+#define SCFT_Q_A 0                /* qa_cu : forward, A block, NsA+1 slices */
+#define SCFT_Q_CB 1               /* qcb_cu: backward, B block, dNsB+1 slices */
+#define SCFT_Q_B 2                /* qb_cu : forward, B block, dNsB+1 slices */
+#define SCFT_Q_CA 3               /* qca_cu: backward, A block, NsA+1 slices */
+
+#define SCFT_MIX_SIMPLE 0         /* phi_w (cuda_aid.cu:382-416) */
+#define SCFT_MIX_ANDERSON 1       /* Anderson mixing on the phi_w residual (no reference counterpart) */
+
+typedef struct scft_ctx scft_ctx;
+
+/* Parameters: the ab.txt keys (init.cpp:86-92) plus the constants the
+ * reference hard-codes (phi_w's wopt/wcmp, cuda_aid.cu:395-396) and the
+ * options that have no reference counterpart (precision, mixing). */
+typedef struct scft_params {
+  int nx, ny, nz;           /* Nx, Ny, Nz: each even, or 1 for ny/nz */
+  double lx, ly, lz;        /* box lengths in Rg */
+  double hAB;               /* xN  (chi N) */
+  double fA;                /* fa  (A fraction) */
+  double ds0;               /* contour step */
+  int batch;                /* independent instances on this device (batch) */
+  int precision;            /* SCFT_PREC_* */
+  double wopt;              /* simple-mixing step, reference 0.05 */
+  double wcmp;              /* incompressibility weight, reference 0.10 */
+  int mixing;               /* SCFT_MIX_* */
+  int anderson_history;     /* Anderson history length (e.g. 20) */
+  double anderson_lambda;   /* Anderson step on the residual */
+  int device;               /* CUDA device ordinal */
+  int reserved[8];          /* must be zero */
+} scft_params;
+
+/* Fill *p with the reference defaults (32^3, box 4, xN 20, fa 0.5,
+ * ds0 0.01, batch 1, FP64, simple mixing wopt 0.05 wcmp 0.10). */
+int scft_params_default(scft_params *p);
+
+/* 1 if the grid is handled by this build's kernels, else 0. */
+int scft_grid_supported(int nx, int ny, int nz);
+
+/* Replaces init_cuda (init_cuda.cu:227-294) + initialize_cufft
+ * (init_cuda.cu:296-546): selects the device, builds the per-axis spectral
+ * tables (init_cuda.cu:394-428), NsA/dNsB (init_cuda.cu:330-331) and
+ * allocates every device buffer.  Fields start at zero. */
+int scft_create(const scft_params *p, scft_ctx **out);
+
+/* Replaces finalize_cufft (init_cuda.cu:551-628).  NULL is ignored. */
+void scft_destroy(scft_ctx *ctx);
+
+/* Message of the last failure on ctx (or of the last failed scft_create
+ * when ctx is NULL).  Never NULL. */
+const char *scft_last_error(const scft_ctx *ctx);
+const char *scft_strerror(int status);
+
+/* Contour discretisation (init_cuda.cu:330-331). */
+int scft_get_ns(const scft_ctx *ctx, int *NsA, int *dNsB);
+
+/* Host -> device copy of one field (the cudaMemcpy of wa/wb at
+ * init_cuda.cu:509-512); src holds batch*M doubles. */
+int scft_set_field(scft_ctx *ctx, int field, const double *src);
+/* Device -> host copy of one field; dst holds batch*M doubles. */
+int scft_get_field(scft_ctx *ctx, int field, double *dst);
+
+/* average_value (cuda_scft.cu:14-59): w -= <w> per instance, on
+ * SCFT_FIELD_WA or SCFT_FIELD_WB. */
+int scft_average_value(scft_ctx *ctx, int field);
+
+/* sovDifFft (cuda_scft.cu:435-563): march propagator `q` (SCFT_Q_*) over
+ * `ns` contour steps in the field `w_field` (SCFT_FIELD_WA/WB) from the
+ * context's qInt buffer; sign=+1 fills slices 0..ns forward, sign=-1 fills
+ * ns..0 backward.  ns must not exceed the propagator's slice count - 1. */
+int scft_sov_dif_fft(scft_ctx *ctx, int q, int w_field, int ns, int sign);
+
+/* qInt hand-offs of getConc: qInt_init (cuda_aid.cu:197-208) when q < 0,
+ * otherwise qInt = slice s of propagator q (qa_to_qInt / qa_to_qInt2,
+ * cuda_aid.cu:170-194). */
+int scft_set_qint(scft_ctx *ctx, int q, int s);
+
+/* Device -> host copy of slice s of propagator q, converted to FP64;
+ * dst holds batch*M doubles. */
+int scft_get_q(scft_ctx *ctx, int q, int s, double *dst);
+
+/* getConc (cuda_scft.cu:61-138): average_value(wa), the four marches, Q and
+ * the trapezoid contour sums giving pha/phb.  Stays on the device. */
+int scft_get_conc(scft_ctx *ctx);
+
+/* Q = ql/M per instance (cuda_scft.cu:118-126); dst holds batch doubles. */
+int scft_get_Q(scft_ctx *ctx, double *dst);
+
+/* phi_w simple mixing (cuda_aid.cu:382-416) with the context's wopt/wcmp. */
+int scft_phi_w(scft_ctx *ctx);
+
+/* The free-energy block of Free (cuda_scft.cu:188-221) on the current
+ * fields: out5 holds batch*5 doubles {F, F_AB, F_W, F_S, inCompMax}. */
+int scft_free_energy(scft_ctx *ctx, double *out5);
+
+/* n_iter iterations of the body of Free (cuda_scft.cu:167-186):
+ * average_value(wa), average_value(wb), getConc, then the field update of
+ * the context's mixing mode.  No host round trip inside.  If out5 is not
+ * NULL the free energy after the last iteration is written to it (batch*5
+ * doubles, the reference's post-update convention). */
+int scft_iterate(scft_ctx *ctx, int n_iter, double *out5);
+
+/* Free (cuda_scft.cu:140-269): max_it iterations; every aver_it iterations
+ * the reference's progress line "GPU %d batch %d: %5d : F, F_AB, F_W,F_S,
+ * inCompMax" is printed to stdout, and every 10*aver_it iterations
+ * pha_<i>.dat is written into `outdir` (NULL: no files).  Returns
+ * SCFT_ERR_NOT_FINITE if F becomes NaN/Inf. */
+int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir);
+
+/* Wait for all work queued on the context's stream. */
+int scft_synchronize(scft_ctx *ctx);
+
+/* Number of kernel launches issued on the context since creation (the
+ * benchmark's gpu_launches evidence). */
+long long scft_launch_count(const scft_ctx *ctx);
+
+/* Timing hook of fft_test (cuda_scft.cu:411-425): run n_iter iterations as
+ * scft_iterate does, bracketed by CUDA events recorded on the context's
+ * stream; *ms receives the elapsed device time. */
+int scft_time_iterations(scft_ctx *ctx, int n_iter, double *ms);
+
+/* Per-march event timing (no reference counterpart).  While enabled, every
+ * propagator march records an event pair on the context's stream;
+ * scft_profile_read returns the summed device time of the marches, their
+ * count and the grid-point x contour-step count they covered, then resets. */
+int scft_profile_enable(scft_ctx *ctx, int enable);
+int scft_profile_read(scft_ctx *ctx, double *march_ms, long long *n_marches,
+                      double *point_steps);
+
+/* ---- file formats (drop-in I/O) ---- */
+
+/* Parse an ab.txt file (init.cpp:81-94) into *p (other fields default). */
+int scft_read_ab_txt(const char *path, scft_params *p, int *intag);
+
+/* Read phi_<idx>.dat (init_cuda.cu:435-456) for instance `inst` of the
+ * context: pha/phb/wa/wb columns after two header lines.  The fields are
+ * uploaded to the device. */
+int scft_read_phi_dat(scft_ctx *ctx, const char *path, int inst);
+
+/* Write pha_<idx>.dat (cuda_scft.cu:233-243) for instance `inst`. */
+int scft_write_pha_dat(scft_ctx *ctx, const char *path, int inst);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCFT_CAPI_H */

@@ -1,0 +1,410 @@
+"""CPU oracle for the diblock-copolymer SCFT hot path.
+
+TEST INFRASTRUCTURE ONLY.  This module is a float64 NumPy restatement of the
+reference's algorithm (ren5885a/SCFT_Ver1.01).  Only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py`` may
+import it, and only as the checker / timed CPU baseline.  The product path
+(the CUDA library behind ``include/scft_capi.h``) never calls it.
+
+Parity pinning: the reference ships no tests, golden vectors or fixtures for
+this path.  The oracle is pinned (a) by known-answer tests derived from the
+mathematics (see ``tests/test_oracle.py``) and (b) against outputs of the
+reference's own CUDA kernels + cuFFT, compiled from the reference sources by
+``oracle/Makefile`` and driven by ``oracle/ref_harness.cpp`` on a GB300; those
+outputs are committed as ``tests/golden/ref_*.npz`` by
+``tests/golden/make_ref_golden.py``.
+
+Every function cites the reference file:line it restates.  Layout: fields are
+``[batch][Nz][Ny][Nx]`` (x fastest), exactly the reference's ``ijk=(k*Ny+j)*Nx+i``
+order (init_cuda.cu:422).  Propagators are returned contour-outer
+``[batch][ns+1][Nz][Ny][Nx]`` (the reference stores them s-fastest,
+``g[b][r][s]``, cuda_aid.cu:237; only the memory order differs).
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# struct.h:11 -- the reference's (truncated) value of pi; kept for parity.
+PI_REF = 3.1415926535
+
+
+@dataclass
+class Params:
+    """The ``ab.txt`` keys (init.cpp:86-92) plus the hard-coded constants.
+
+    ``wopt``/``wcmp`` are the simple-mixing constants hard-coded in
+    ``phi_w`` (cuda_aid.cu:395-396); ``aver_it`` is ``AverIt`` (init.cpp:39).
+    """
+
+    nx: int = 32
+    ny: int = 32
+    nz: int = 32
+    lx: float = 4.0
+    ly: float = 4.0
+    lz: float = 4.0
+    hAB: float = 20.0          # xN
+    fA: float = 0.5            # fa
+    ds0: float = 0.01
+    batch: int = 1             # Num_SCFT
+    intag: int = 1024
+    wopt: float = 0.05
+    wcmp: float = 0.10
+    aver_it: int = 10
+
+    @property
+    def shape(self):
+        return (self.nz, self.ny, self.nx)
+
+    @property
+    def M(self):
+        return self.nx * self.ny * self.nz
+
+    @property
+    def NsA(self):
+        # init_cuda.cu:330
+        return int(self.fA / self.ds0 + 1.0e-8)
+
+    @property
+    def dNsB(self):
+        # init_cuda.cu:329,331 (dfB = 1 - fA)
+        return int((1.0 - self.fA) / self.ds0 + 1.0e-8)
+
+    @property
+    def ds2(self):
+        # init_cuda.cu:328
+        return self.ds0 / 2
+
+
+# ---------------------------------------------------------------- config I/O
+
+def parse_ab_txt(text: str) -> Params:
+    """Parse the ``ab.txt`` format read at init.cpp:86-92."""
+    p = Params()
+    vals = {}
+    for line in text.splitlines():
+        for part in line.split(","):
+            if "=" in part:
+                k, v = part.split("=", 1)
+                vals[k.strip()] = v.strip()
+    p.intag = int(vals["intag"])
+    p.hAB = float(vals["xN"])
+    p.fA = float(vals["fa"])
+    p.lx, p.ly, p.lz = float(vals["lx"]), float(vals["ly"]), float(vals["lz"])
+    p.nx, p.ny, p.nz = int(vals["Nx"]), int(vals["Ny"]), int(vals["Nz"])
+    p.ds0 = float(vals["ds0"])
+    p.batch = int(vals["batch"])
+    return p
+
+
+def format_g(x: float) -> str:
+    """C printf ``%g`` (6 significant digits)."""
+    return "%g" % x
+
+
+def write_pha_dat(path, p: Params, pha, phb, wa, wb):
+    """Writer of ``pha_%d.dat`` (cuda_scft.cu:233-243)."""
+    dx, dy, dz = p.lx / p.nx, p.ly / p.ny, p.lz / p.nz
+    with open(path, "w") as f:
+        f.write("Nx=%d, Ny=%d, Nz=%d\n" % (p.nx, p.ny, p.nz))
+        f.write("dx=%g, dy=%g, dz=%g\n" % (dx, dy, dz))
+        for a, b, c, d in zip(pha.ravel(), phb.ravel(), wa.ravel(), wb.ravel()):
+            f.write("%g %g %g %g\n" % (a, b, c, d))
+
+
+def read_phi_dat(path, M):
+    """Reader of ``phi_%d.dat`` (init_cuda.cu:435-456): 2 header lines, then
+    M lines ``pha phb wa wb``."""
+    with open(path) as f:
+        f.readline()
+        f.readline()
+        data = np.loadtxt(f, max_rows=M)
+    data = data.reshape(M, 4)
+    return data[:, 0].copy(), data[:, 1].copy(), data[:, 2].copy(), data[:, 3].copy()
+
+
+# ----------------------------------------------------------- spectral tables
+
+def k2_axis(n: int, length: float) -> np.ndarray:
+    """Squared wave numbers of one axis (init_cuda.cu:398-418).
+
+    Bins ``i <= n/2-1`` get ``+i``, bins ``i >= n/2`` get ``i-n`` (so a
+    length-1 axis gets ``-1``: the reference's Nz=1 behaviour).
+    """
+    d = length / n
+    k = np.empty(n)
+    for i in range(0, n // 2):
+        k[i] = 2 * PI_REF * i * 1.0 / n / d
+    for i in range(n // 2, n):
+        k[i] = 2 * PI_REF * (i - n) * 1.0 / d / n
+    return k * k
+
+
+def kxyzdz(p: Params) -> np.ndarray:
+    """``kxyzdz[k][j][i] = exp(-ds0*(kx2[i]+ky2[j]+kz2[k]))`` (init_cuda.cu:420-428)."""
+    kx = k2_axis(p.nx, p.lx)
+    ky = k2_axis(p.ny, p.ly)
+    kz = k2_axis(p.nz, p.lz)
+    ksq = (kx[None, None, :] + ky[None, :, None]) + kz[:, None, None]
+    return np.exp(-p.ds0 * ksq)
+
+
+def kxyzdz_half(p: Params) -> np.ndarray:
+    """The table as ``sufaceField_go`` indexes it for the D2Z half spectrum:
+    ``ijkr = ix + iy*Nx + iz*Nx*Ny`` with ``ix < Nx/2+1`` (cuda_aid.cu:312-325)."""
+    return kxyzdz(p)[:, :, : p.nx // 2 + 1]
+
+
+# ------------------------------------------------------------ hot-path steps
+
+def average_value(w: np.ndarray) -> np.ndarray:
+    """``average_value`` (cuda_scft.cu:14-59): per instance, ``w -= sum(w)/M``
+    (reduce3, cuda_aid.cuh:36-80, then minus_average, cuda_aid.cu:365-380)."""
+    b = w.shape[0]
+    flat = w.reshape(b, -1)
+    s = flat.sum(axis=1)
+    return (flat - (s / flat.shape[1])[:, None]).reshape(w.shape)
+
+
+def sov_dif_fft(q_init: np.ndarray, w: np.ndarray, ns: int, sign: int, p: Params,
+                kdz_half: np.ndarray | None = None) -> np.ndarray:
+    """One propagator march (``sovDifFft``, cuda_scft.cu:435-563).
+
+    ``q_init``/``w``: ``[batch][Nz][Ny][Nx]``.  Returns ``[batch][ns+1][...]``.
+    sign=+1: q[0]=q_init, for iz=1..ns: q[iz] from q[iz-1] (cuda_scft.cu:458-494).
+    sign=-1: q[ns]=q_init, for iz=ns-1..0: q[iz] from q[iz+1] (:506-545).
+    Each step: in = q*wdz (initilize_in_go, cuda_aid.cu:227-241); D2Z;
+    out *= kxyzdz (sufaceField_go, :306-328); Z2D; q = in*wdz/M
+    (in_to_g_go, :346-361).  numpy's irfftn includes the 1/M.
+    """
+    if kdz_half is None:
+        kdz_half = kxyzdz_half(p)
+    wdz = np.exp(-w * p.ds2)                    # initilize_wdz, cuda_aid.cu:242-257
+    b = w.shape[0]
+    q = np.empty((b, ns + 1) + p.shape)
+    axes = (1, 2, 3)
+    if sign == 1:
+        q[:, 0] = q_init                        # initilize_q, cuda_aid.cu:259-272
+        order = [(iz, iz - 1) for iz in range(1, ns + 1)]
+    elif sign == -1:
+        q[:, ns] = q_init                       # initilize_q_inverse, cuda_aid.cu:274-287
+        order = [(iz, iz + 1) for iz in range(ns - 1, -1, -1)]
+    else:
+        raise ValueError("sign must be +1 or -1")
+    for dst, src in order:
+        spec = np.fft.rfftn(q[:, src] * wdz, axes=axes)
+        spec *= kdz_half[None]
+        q[:, dst] = np.fft.irfftn(spec, s=p.shape, axes=axes) * wdz
+    return q
+
+
+@dataclass
+class Conc:
+    pha: np.ndarray
+    phb: np.ndarray
+    Q: np.ndarray            # per instance, ql/M (cuda_scft.cu:124)
+    qa: np.ndarray
+    qcb: np.ndarray
+    qb: np.ndarray
+    qca: np.ndarray
+    wa: np.ndarray           # wa after getConc's own average_value (cuda_scft.cu:71)
+
+
+def trapezoid_sum(q: np.ndarray, qc: np.ndarray) -> np.ndarray:
+    """Contour sum of ``w_to_phi_go`` (cuda_aid.cu:87-107): weights 1/2 at both
+    ends, 1 inside.  ``q``/``qc``: ``[batch][ns+1][...]``."""
+    prod = q * qc
+    if prod.shape[1] == 1:          # ns == 0: iz==0 is also iz==ns (cuda_aid.cu:91)
+        return 0.5 * prod[:, 0]
+    s = 0.5 * prod[:, 0] + 0.5 * prod[:, -1]
+    if prod.shape[1] > 2:
+        s = s + prod[:, 1:-1].sum(axis=1)
+    return s
+
+
+def get_conc(wa: np.ndarray, wb: np.ndarray, p: Params, kdz_half=None) -> Conc:
+    """``getConc`` (cuda_scft.cu:61-138)."""
+    if kdz_half is None:
+        kdz_half = kxyzdz_half(p)
+    wa = average_value(wa)                                    # :71
+    ones = np.ones_like(wa)                                   # qInt_init, :77
+    qa = sov_dif_fft(ones, wa, p.NsA, +1, p, kdz_half)        # :83
+    qcb = sov_dif_fft(ones, wb, p.dNsB, -1, p, kdz_half)      # :86
+    qb = sov_dif_fft(qa[:, p.NsA], wb, p.dNsB, +1, p, kdz_half)   # qa_to_qInt :93, :99
+    qca = sov_dif_fft(qcb[:, 0], wa, p.NsA, -1, p, kdz_half)      # qa_to_qInt2 :106, :112
+    b = wa.shape[0]
+    ql = qb[:, p.dNsB].reshape(b, -1).sum(axis=1)             # cal_ql, :118
+    Q = ql / p.M                                              # :124
+    ffl = p.ds0 / Q                                           # :125
+    pha = ffl[:, None, None, None] * trapezoid_sum(qa, qca)   # w_to_phi_go, :130
+    phb = ffl[:, None, None, None] * trapezoid_sum(qb, qcb)
+    return Conc(pha, phb, Q, qa, qcb, qb, qca, wa)
+
+
+def phi_w(wa, wb, pha, phb, hAB, wopt=0.05, wcmp=0.10):
+    """Simple mixing (``phi_w``, cuda_aid.cu:382-416).  Returns the updated
+    fields and the residuals (waDiff, wbDiff) before scaling by wopt."""
+    eta = (wa + wb - hAB) / 2
+    psum = 1.0 - pha - phb
+    wad = hAB * phb + eta - wa
+    wbd = hAB * pha + eta - wb
+    wad = wad - wcmp * psum
+    wbd = wbd - wcmp * psum
+    return wa + wopt * wad, wb + wopt * wbd, wad, wbd
+
+
+def free_energy(wa, wb, pha, phb, Q, hAB):
+    """The free-energy block of ``Free`` (cuda_scft.cu:190-221), per instance:
+    returns (F, F_AB, F_W, F_S, inCompMax)."""
+    b = wa.shape[0]
+    pa, pb = pha.reshape(b, -1), phb.reshape(b, -1)
+    a, bb = wa.reshape(b, -1), wb.reshape(b, -1)
+    M = pa.shape[1]
+    incomp = np.abs(1 - pa - pb).max(axis=1)
+    fAB = (hAB * pa * pb).sum(axis=1) / M
+    fW = -(a * pa + bb * pb).sum(axis=1) / M
+    fS = -np.log(Q)
+    return fAB + fW + fS, fAB, fW, fS, incomp
+
+
+@dataclass
+class FreeResult:
+    wa: np.ndarray
+    wb: np.ndarray
+    pha: np.ndarray
+    phb: np.ndarray
+    Q: np.ndarray
+    log: list = field(default_factory=list)   # (iter, b, F, FAB, FW, FS, incomp)
+
+
+def free_loop(wa, wb, p: Params, max_it: int, writer=None) -> FreeResult:
+    """``Free`` (cuda_scft.cu:140-269): ``max_it`` SCF iterations of
+    average_value(wa), average_value(wb), getConc, phi_w; every ``AverIt``
+    iterations the free energy (computed with the *updated* w and the
+    pre-update phi and Q, as the reference does) is logged; every
+    ``10*AverIt`` iterations ``writer(iter, b, pha, phb, wa, wb)`` is called
+    (the pha_%d.dat dump, :233-243)."""
+    kdz = kxyzdz_half(p)
+    res = FreeResult(wa, wb, None, None, None)
+    pha = phb = Q = None
+    for it in range(1, max_it + 1):
+        wa = average_value(wa)                                 # :170
+        wb = average_value(wb)                                 # :172
+        c = get_conc(wa, wb, p, kdz)                           # :174
+        wa, pha, phb, Q = c.wa, c.pha, c.phb, c.Q
+        wa, wb, _, _ = phi_w(wa, wb, pha, phb, p.hAB, p.wopt, p.wcmp)   # :182
+        if it % p.aver_it == 0:
+            F, fAB, fW, fS, inc = free_energy(wa, wb, pha, phb, Q, p.hAB)
+            for b in range(wa.shape[0]):
+                res.log.append((it, b, F[b], fAB[b], fW[b], fS[b], inc[b]))
+            if writer is not None and it % (p.aver_it * 10) == 0:
+                for b in range(wa.shape[0]):
+                    writer(it, b, pha[b], phb[b], wa[b], wb[b])
+    res.wa, res.wb, res.pha, res.phb, res.Q = wa, wb, pha, phb, Q
+    return res
+
+
+def format_free_line(gpu_index, b, it, F, fAB, fW, fS, inc):
+    """The progress line printed at cuda_scft.cu:221."""
+    return "GPU %d batch %d: %5d : %.8e, %.8e, %.8e,%.8e, %.8e" % (
+        gpu_index, b, it, F, fAB, fW, fS, inc)
+
+
+# ---------------------------------------------------- CPU baseline (timed)
+
+def march_rate_cpu(p: Params, w: np.ndarray, n_steps: int, workers: int | None = None):
+    """Timed CPU baseline of the same step (scipy.fft, pocketfft, threaded):
+    ``n_steps`` forward split steps of one propagator over ``w``.  Returns
+    (seconds, point_steps).  Used only by bench.py's CPU-baseline legs."""
+    import time
+    import scipy.fft as sfft
+    workers = workers or os.cpu_count()
+    kdz = kxyzdz_half(p)[None]
+    wdz = np.exp(-w * p.ds2)
+    q = np.ones_like(w)
+    axes = (1, 2, 3)
+    t0 = time.perf_counter()
+    for _ in range(n_steps):
+        spec = sfft.rfftn(q * wdz, axes=axes, workers=workers)
+        spec *= kdz
+        q = sfft.irfftn(spec, s=p.shape, axes=axes, workers=workers) * wdz
+    dt = time.perf_counter() - t0
+    return dt, n_steps * w.size
+
+
+def iteration_cpu(wa, wb, p: Params, workers: int | None = None):
+    """One full SCF iteration with scipy.fft (same arithmetic as free_loop's
+    body, threaded FFTs).  Used only by bench.py's CPU-baseline legs."""
+    import scipy.fft as sfft
+    workers = workers or os.cpu_count()
+    kdz = kxyzdz_half(p)[None]
+    axes = (1, 2, 3)
+
+    def march(q0, w, ns, sign):
+        wdz = np.exp(-w * p.ds2)
+        q = np.empty((w.shape[0], ns + 1) + p.shape)
+        if sign == 1:
+            q[:, 0] = q0
+            order = [(i, i - 1) for i in range(1, ns + 1)]
+        else:
+            q[:, ns] = q0
+            order = [(i, i + 1) for i in range(ns - 1, -1, -1)]
+        for dst, src in order:
+            spec = sfft.rfftn(q[:, src] * wdz, axes=axes, workers=workers)
+            spec *= kdz
+            q[:, dst] = sfft.irfftn(spec, s=p.shape, axes=axes, workers=workers) * wdz
+        return q
+
+    wa = average_value(average_value(wa))
+    wb = average_value(wb)
+    ones = np.ones_like(wa)
+    qa = march(ones, wa, p.NsA, 1)
+    qcb = march(ones, wb, p.dNsB, -1)
+    qb = march(qa[:, p.NsA], wb, p.dNsB, 1)
+    qca = march(qcb[:, 0], wa, p.NsA, -1)
+    Q = qb[:, p.dNsB].reshape(wa.shape[0], -1).sum(axis=1) / p.M
+    ffl = p.ds0 / Q
+    pha = ffl[:, None, None, None] * trapezoid_sum(qa, qca)
+    phb = ffl[:, None, None, None] * trapezoid_sum(qb, qcb)
+    wa, wb, _, _ = phi_w(wa, wb, pha, phb, p.hAB, p.wopt, p.wcmp)
+    return wa, wb, pha, phb, Q
+
+
+def pt_steps_per_iteration(p: Params) -> int:
+    """Grid points x contour steps of one SCF iteration: the four marches
+    take NsA + dNsB + dNsB + NsA steps over batch*M points."""
+    return 2 * (p.NsA + p.dNsB) * p.M * p.batch
+
+
+def reduce3_quirk_sum(x: np.ndarray, threads: int) -> float:
+    """The reference's ``reduce3`` block sum (cuda_aid.cuh:36-80) for a thread
+    count that is not a power of two: the shared-memory tree halving drops
+    elements, so the result differs from the true sum.  Used to document the
+    quirk; the GPU path computes the true sum."""
+    n = x.size
+    chunk = n // threads + 1
+    sdata = np.zeros(threads)
+    for t in range(threads):
+        lo = t * chunk
+        hi = min(lo + chunk, n)
+        if lo < n:
+            sdata[t] = x[lo:hi].sum()
+    s = threads // 2
+    while s > 0:
+        sdata[:s] = sdata[:s] + sdata[s:2 * s]
+        s >>= 1
+    return float(sdata[0])
+
+
+def factor_decompose_1024(n: int) -> int:
+    """Largest divisor of n that is <= 1024 (what factor_decompose_1024,
+    init_cuda.cu:24-80, computes: the thread count of the reference's
+    reductions and elementwise kernels)."""
+    best = 1
+    for d in range(1, min(n, 1024) + 1):
+        if n % d == 0:
+            best = d
+    return best

@@ -1,0 +1,279 @@
+"""GB300-native diblock-copolymer SCFT hot path: Python host mirror.
+
+A thin ctypes layer over the C ABI of ``include/scft_capi.h`` (the CUDA
+library ``libscft_gb300.so`` built in-tree by ``build.py``).  Method names
+follow the reference's C++ API (``average_value``, ``sov_dif_fft``,
+``get_conc``, ``phi_w``, ``free``), arrays are float64 numpy arrays shaped
+``[batch, Nz, Ny, Nx]``.  There is no CPU fallback: if the library is
+missing, loading raises.
+
+The directory name is not a Python identifier; import it with
+``load_package()`` from ``__graft_entry__`` (registered as ``scft_gb300``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libscft_gb300.so")
+
+OK = 0
+ERR_INVALID_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NO_MEMORY = 1, 2, 3, 4
+ERR_NOT_FINITE, ERR_IO, ERR_NO_DEVICE = 5, 6, 7
+PREC_FP64, PREC_FP32 = 0, 1
+FIELD_WA, FIELD_WB, FIELD_PHA, FIELD_PHB = 0, 1, 2, 3
+Q_A, Q_CB, Q_B, Q_CA = 0, 1, 2, 3
+MIX_SIMPLE, MIX_ANDERSON = 0, 1
+
+# Every symbol include/scft_capi.h declares (checked by the CPU tests).
+EXPORTS = [
+    "scft_params_default", "scft_grid_supported", "scft_create", "scft_destroy",
+    "scft_last_error", "scft_strerror", "scft_get_ns", "scft_set_field", "scft_get_field",
+    "scft_average_value", "scft_sov_dif_fft", "scft_set_qint", "scft_get_q", "scft_get_conc",
+    "scft_get_Q", "scft_phi_w", "scft_free_energy", "scft_iterate", "scft_free",
+    "scft_synchronize", "scft_launch_count", "scft_read_ab_txt", "scft_read_phi_dat",
+    "scft_write_pha_dat", "scft_time_iterations", "scft_profile_enable", "scft_profile_read",
+]
+
+
+class ScftParams(C.Structure):
+    """Mirror of ``scft_params`` (include/scft_capi.h)."""
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
+        ("hAB", C.c_double), ("fA", C.c_double), ("ds0", C.c_double),
+        ("batch", C.c_int), ("precision", C.c_int),
+        ("wopt", C.c_double), ("wcmp", C.c_double),
+        ("mixing", C.c_int), ("anderson_history", C.c_int), ("anderson_lambda", C.c_double),
+        ("device", C.c_int), ("reserved", C.c_int * 8),
+    ]
+
+
+class ScftError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"scft status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"{p} is missing: run __graft_entry__.build() (no CPU fallback exists)")
+    lib = C.CDLL(p)
+    dp = C.POINTER(C.c_double)
+    vp = C.c_void_p
+    sig = {
+        "scft_params_default": (C.c_int, [C.POINTER(ScftParams)]),
+        "scft_grid_supported": (C.c_int, [C.c_int, C.c_int, C.c_int]),
+        "scft_create": (C.c_int, [C.POINTER(ScftParams), C.POINTER(vp)]),
+        "scft_destroy": (None, [vp]),
+        "scft_last_error": (C.c_char_p, [vp]),
+        "scft_strerror": (C.c_char_p, [C.c_int]),
+        "scft_get_ns": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "scft_set_field": (C.c_int, [vp, C.c_int, dp]),
+        "scft_get_field": (C.c_int, [vp, C.c_int, dp]),
+        "scft_average_value": (C.c_int, [vp, C.c_int]),
+        "scft_sov_dif_fft": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+        "scft_set_qint": (C.c_int, [vp, C.c_int, C.c_int]),
+        "scft_get_q": (C.c_int, [vp, C.c_int, C.c_int, dp]),
+        "scft_get_conc": (C.c_int, [vp]),
+        "scft_get_Q": (C.c_int, [vp, dp]),
+        "scft_phi_w": (C.c_int, [vp]),
+        "scft_free_energy": (C.c_int, [vp, dp]),
+        "scft_iterate": (C.c_int, [vp, C.c_int, dp]),
+        "scft_free": (C.c_int, [vp, C.c_int, C.c_int, C.c_char_p]),
+        "scft_synchronize": (C.c_int, [vp]),
+        "scft_launch_count": (C.c_longlong, [vp]),
+        "scft_read_ab_txt": (C.c_int, [C.c_char_p, C.POINTER(ScftParams), C.POINTER(C.c_int)]),
+        "scft_read_phi_dat": (C.c_int, [vp, C.c_char_p, C.c_int]),
+        "scft_write_pha_dat": (C.c_int, [vp, C.c_char_p, C.c_int]),
+        "scft_time_iterations": (C.c_int, [vp, C.c_int, dp]),
+        "scft_profile_enable": (C.c_int, [vp, C.c_int]),
+        "scft_profile_read": (C.c_int, [vp, dp, C.POINTER(C.c_longlong), dp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def default_params(**kw) -> ScftParams:
+    lib = load_library()
+    p = ScftParams()
+    lib.scft_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+def read_ab_txt(path: str):
+    """Parse ``ab.txt`` (init.cpp:81-94) -> (ScftParams, intag)."""
+    lib = load_library()
+    p = ScftParams()
+    tag = C.c_int(0)
+    st = lib.scft_read_ab_txt(path.encode(), C.byref(p), C.byref(tag))
+    if st != OK:
+        raise ScftError(st, lib.scft_last_error(None).decode())
+    return p, tag.value
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Context:
+    """One device context: ``batch`` instances of one grid (scft_ctx)."""
+
+    def __init__(self, params: ScftParams | None = None, **kw):
+        self.lib = load_library()
+        self.params = params if params is not None else default_params(**kw)
+        if params is not None:
+            for k, v in kw.items():
+                setattr(self.params, k, v)
+        h = C.c_void_p()
+        st = self.lib.scft_create(C.byref(self.params), C.byref(h))
+        if st != OK:
+            raise ScftError(st, self.lib.scft_last_error(None).decode())
+        self.h = h
+        a, b = C.c_int(), C.c_int()
+        self.lib.scft_get_ns(self.h, C.byref(a), C.byref(b))
+        self.NsA, self.dNsB = a.value, b.value
+        p = self.params
+        self.shape = (p.batch, p.nz, p.ny, p.nx)
+
+    # -- plumbing
+    def _ck(self, st):
+        if st != OK:
+            raise ScftError(st, self.lib.scft_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.scft_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- fields
+    def set_field(self, field: int, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(self.shape)
+        self._ck(self.lib.scft_set_field(self.h, field, _dptr(a)))
+
+    def get_field(self, field: int) -> np.ndarray:
+        out = np.empty(self.shape)
+        self._ck(self.lib.scft_get_field(self.h, field, _dptr(out)))
+        return out
+
+    def set_w(self, wa, wb):
+        self.set_field(FIELD_WA, wa)
+        self.set_field(FIELD_WB, wb)
+
+    @property
+    def wa(self):
+        return self.get_field(FIELD_WA)
+
+    @property
+    def wb(self):
+        return self.get_field(FIELD_WB)
+
+    @property
+    def pha(self):
+        return self.get_field(FIELD_PHA)
+
+    @property
+    def phb(self):
+        return self.get_field(FIELD_PHB)
+
+    # -- hot path (reference API names)
+    def average_value(self, field: int):
+        self._ck(self.lib.scft_average_value(self.h, field))
+
+    def set_qint(self, q: int = -1, s: int = 0):
+        self._ck(self.lib.scft_set_qint(self.h, q, s))
+
+    def sov_dif_fft(self, q: int, w_field: int, ns: int, sign: int):
+        self._ck(self.lib.scft_sov_dif_fft(self.h, q, w_field, ns, sign))
+
+    def get_q(self, q: int, s: int) -> np.ndarray:
+        out = np.empty(self.shape)
+        self._ck(self.lib.scft_get_q(self.h, q, s, _dptr(out)))
+        return out
+
+    def get_conc(self):
+        self._ck(self.lib.scft_get_conc(self.h))
+
+    def Q(self) -> np.ndarray:
+        out = np.empty(self.shape[0])
+        self._ck(self.lib.scft_get_Q(self.h, _dptr(out)))
+        return out
+
+    def phi_w(self):
+        self._ck(self.lib.scft_phi_w(self.h))
+
+    def free_energy(self) -> np.ndarray:
+        out = np.empty((self.shape[0], 5))
+        self._ck(self.lib.scft_free_energy(self.h, _dptr(out)))
+        return out
+
+    def iterate(self, n: int, with_energy: bool = False):
+        if with_energy:
+            out = np.empty((self.shape[0], 5))
+            self._ck(self.lib.scft_iterate(self.h, n, _dptr(out)))
+            return out
+        self._ck(self.lib.scft_iterate(self.h, n, None))
+        return None
+
+    def free(self, max_it: int, aver_it: int = 10, outdir: str | None = None):
+        self._ck(self.lib.scft_free(self.h, max_it, aver_it,
+                                    outdir.encode() if outdir else None))
+
+    def synchronize(self):
+        self._ck(self.lib.scft_synchronize(self.h))
+
+    def launch_count(self) -> int:
+        return int(self.lib.scft_launch_count(self.h))
+
+    def time_iterations(self, n: int) -> float:
+        """Device milliseconds of n SCF iterations (events on the library's stream)."""
+        ms = C.c_double()
+        self._ck(self.lib.scft_time_iterations(self.h, n, C.byref(ms)))
+        return ms.value
+
+    def profile_enable(self, reserve_marches: int):
+        self._ck(self.lib.scft_profile_enable(self.h, reserve_marches))
+
+    def profile_read(self):
+        """-> (summed march milliseconds, number of marches, point-steps)."""
+        ms, n, ps = C.c_double(), C.c_longlong(), C.c_double()
+        self._ck(self.lib.scft_profile_read(self.h, C.byref(ms), C.byref(n), C.byref(ps)))
+        return ms.value, n.value, ps.value
+
+    def read_phi_dat(self, path: str, inst: int = 0):
+        self._ck(self.lib.scft_read_phi_dat(self.h, path.encode(), inst))
+
+    def write_pha_dat(self, path: str, inst: int = 0):
+        self._ck(self.lib.scft_write_pha_dat(self.h, path.encode(), inst))

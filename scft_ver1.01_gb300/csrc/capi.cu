@@ -1,0 +1,620 @@
+// C ABI of the SCFT hot path (include/scft_capi.h): context set-up, the
+// propagator march, getConc, mixing, free energy and the SCF loop.  Host
+// code only; kernels live in k_line.cu / k_fields.cu.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "ctx.h"
+
+using scft::AxisPlan;
+
+namespace {
+
+// struct.h:11 -- the reference's value of pi, used for the wave numbers.
+constexpr double kPiRef = 3.1415926535;
+
+std::string g_create_err = "no error";
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return scft_fail(ctx, SCFT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define CKL(call)                                                                       \
+  do {                                                                                  \
+    ++ctx->launches;                                                                    \
+    CK(call);                                                                           \
+  } while (0)
+
+// Squared wave numbers of one axis, in the reference's order of operations
+// (init_cuda.cu:398-418): bins i <= n/2-1 are +i, bins i >= n/2 are i-n.
+std::vector<double> k2_axis(int n, double L) {
+  std::vector<double> k(n);
+  const double d = L / n;
+  for (int i = 0; i <= n / 2 - 1; ++i) k[i] = 2 * kPiRef * i * 1.0 / n / d;
+  for (int i = n / 2; i < n; ++i) k[i] = 2 * kPiRef * (i - n) * 1.0 / d / n;
+  for (int i = 0; i < n; ++i) k[i] *= k[i];
+  return k;
+}
+
+bool radix_plan(int n, int *fac, int *nfac) {
+  int m = n, k = 0;
+  while (m % 4 == 0) { fac[k++] = 4; m /= 4; }
+  while (m % 2 == 0) { fac[k++] = 2; m /= 2; }
+  for (int p = 3; p <= 61 && m > 1; p += 2) {
+    while (m % p == 0) {
+      if (k >= 24) return false;
+      fac[k++] = p;
+      m /= p;
+    }
+  }
+  *nfac = k;
+  return m == 1;
+}
+
+bool axis_ok(int n, bool allow_one) {
+  if (n == 1) return allow_one;
+  if (n < 2 || (n & 1)) return false;
+  if (n > 4096) return false;
+  int fac[24], nf;
+  return radix_plan(n, fac, &nf);
+}
+
+template <typename R>
+int march_t(scft_ctx *ctx, int qi, const double *w, int ns, int sign) {
+  const long long M = ctx->M;
+  const int B = ctx->batch;
+  R *q = static_cast<R *>(ctx->q[qi]);
+  const long long qbs = (long long)(ctx->q_ns[qi] + 1) * M;
+  R *W = static_cast<R *>(ctx->W);
+  R *qint = static_cast<R *>(ctx->qint);
+  R *tmp[2] = {static_cast<R *>(ctx->tmp[0]), static_cast<R *>(ctx->tmp[1])};
+  // initilize_wdz (cuda_scft.cu:450)
+  CKL(scft::launch_boltzmann<R>(w, W, M * B, ctx->p.ds0 / 2, ctx->st));
+  // initilize_q / initilize_q_inverse (cuda_scft.cu:463,513)
+  const int s0 = sign > 0 ? 0 : ns;
+  CKL(scft::launch_copy_slice<R>(q + (long long)s0 * M, qbs, qint, M, M, B, ctx->st));
+  const int np = (int)ctx->passes.size();
+  for (int it = 1; it <= ns; ++it) {
+    const int dst = sign > 0 ? it : ns - it;
+    const int src = sign > 0 ? dst - 1 : dst + 1;
+    for (int pi = 0; pi < np; ++pi) {
+      const R *in = pi == 0 ? q + (long long)src * M : tmp[(pi - 1) & 1];
+      const long long ibs = pi == 0 ? qbs : M;
+      R *out = pi == np - 1 ? q + (long long)dst * M : tmp[pi & 1];
+      const long long obs = pi == np - 1 ? qbs : M;
+      CKL(scft::launch_line_filter<R>(ctx->passes[pi], in, ibs, out, obs, pi == 0 ? W : nullptr,
+                                      pi == np - 1 ? W : nullptr, M, B, ctx->st));
+    }
+  }
+  return SCFT_OK;
+}
+
+int prof_reserve(scft_ctx *ctx, size_t n_events) {
+  while (ctx->prof_events.size() < n_events) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    ctx->prof_events.push_back(e);
+  }
+  return SCFT_OK;
+}
+
+int march(scft_ctx *ctx, int qi, int w_field, int ns, int sign) {
+  const double *w = w_field == SCFT_FIELD_WA ? ctx->wa : ctx->wb;
+  int rc;
+  if (ctx->profiling) {
+    if ((rc = prof_reserve(ctx, ctx->prof_used + 2))) return rc;
+    CK(cudaEventRecord(ctx->prof_events[ctx->prof_used], ctx->st));
+  }
+  rc = ctx->rbytes == 4 ? march_t<float>(ctx, qi, w, ns, sign)
+                        : march_t<double>(ctx, qi, w, ns, sign);
+  if (rc) return rc;
+  if (ctx->profiling) {
+    CK(cudaEventRecord(ctx->prof_events[ctx->prof_used + 1], ctx->st));
+    ctx->prof_used += 2;
+    ctx->prof_point_steps += (double)ns * ctx->M * ctx->batch;
+  }
+  return SCFT_OK;
+}
+
+int average(scft_ctx *ctx, double *data) {
+  CKL(scft::launch_partial_sum<double>(data, ctx->M, ctx->M, ctx->batch, ctx->partial, ctx->nblk,
+                                       ctx->st));
+  CKL(scft::launch_finalize_sum(ctx->partial, ctx->nblk, ctx->batch, 1.0, ctx->sum, ctx->st));
+  CKL(scft::launch_minus_average(data, ctx->sum, ctx->M, ctx->batch, ctx->st));
+  return SCFT_OK;
+}
+
+int set_qint(scft_ctx *ctx, int qi, int s) {
+  const long long M = ctx->M;
+  if (qi < 0) {
+    if (ctx->rbytes == 4)
+      CKL(scft::launch_fill<float>(static_cast<float *>(ctx->qint), M, 1.0f, M, ctx->batch, ctx->st));
+    else
+      CKL(scft::launch_fill<double>(static_cast<double *>(ctx->qint), M, 1.0, M, ctx->batch, ctx->st));
+    return SCFT_OK;
+  }
+  const long long qbs = (long long)(ctx->q_ns[qi] + 1) * M;
+  if (ctx->rbytes == 4)
+    CKL(scft::launch_copy_slice<float>(static_cast<float *>(ctx->qint), M,
+                                       static_cast<float *>(ctx->q[qi]) + (long long)s * M, qbs,
+                                       M, ctx->batch, ctx->st));
+  else
+    CKL(scft::launch_copy_slice<double>(static_cast<double *>(ctx->qint), M,
+                                        static_cast<double *>(ctx->q[qi]) + (long long)s * M, qbs,
+                                        M, ctx->batch, ctx->st));
+  return SCFT_OK;
+}
+
+template <typename R>
+int q_and_phi(scft_ctx *ctx) {
+  const long long M = ctx->M;
+  const int B = ctx->batch;
+  // cal_ql on qb[dNsB] (cuda_scft.cu:118), then ql/M and ffl=ds0/Q (:123-126)
+  const R *qb = static_cast<const R *>(ctx->q[SCFT_Q_B]);
+  const long long qbs = (long long)(ctx->q_ns[SCFT_Q_B] + 1) * M;
+  CKL(scft::launch_partial_sum<R>(qb + (long long)ctx->dNsB * M, qbs, M, B, ctx->partial,
+                                  ctx->nblk, ctx->st));
+  CKL(scft::launch_finalize_sum(ctx->partial, ctx->nblk, B, 1.0, ctx->sum, ctx->st));
+  CKL(scft::launch_q_ffl(ctx->sum, M, ctx->p.ds0, B, ctx->Q, ctx->ffl, ctx->st));
+  // w_to_phi_go (cuda_scft.cu:130)
+  CKL(scft::launch_contour_phi<R>(static_cast<const R *>(ctx->q[SCFT_Q_A]),
+                                  static_cast<const R *>(ctx->q[SCFT_Q_CA]), ctx->NsA, M, B,
+                                  ctx->ffl, ctx->pha, ctx->st));
+  CKL(scft::launch_contour_phi<R>(static_cast<const R *>(ctx->q[SCFT_Q_B]),
+                                  static_cast<const R *>(ctx->q[SCFT_Q_CB]), ctx->dNsB, M, B,
+                                  ctx->ffl, ctx->phb, ctx->st));
+  return SCFT_OK;
+}
+
+int get_conc(scft_ctx *ctx) {
+  int rc;
+  if ((rc = average(ctx, ctx->wa))) return rc;                                 // :71
+  if ((rc = set_qint(ctx, -1, 0))) return rc;                                  // :77
+  if ((rc = march(ctx, SCFT_Q_A, SCFT_FIELD_WA, ctx->NsA, 1))) return rc;      // :83
+  if ((rc = march(ctx, SCFT_Q_CB, SCFT_FIELD_WB, ctx->dNsB, -1))) return rc;   // :86
+  if ((rc = set_qint(ctx, SCFT_Q_A, ctx->NsA))) return rc;                     // :93
+  if ((rc = march(ctx, SCFT_Q_B, SCFT_FIELD_WB, ctx->dNsB, 1))) return rc;     // :99
+  if ((rc = set_qint(ctx, SCFT_Q_CB, 0))) return rc;                           // :106
+  if ((rc = march(ctx, SCFT_Q_CA, SCFT_FIELD_WA, ctx->NsA, -1))) return rc;    // :112
+  return ctx->rbytes == 4 ? q_and_phi<float>(ctx) : q_and_phi<double>(ctx);
+}
+
+int mix(scft_ctx *ctx) {
+  CKL(scft::launch_phi_w(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->p.wopt,
+                         ctx->p.wcmp, ctx->M, ctx->batch, ctx->st));
+  return SCFT_OK;
+}
+
+int free_energy_dev(scft_ctx *ctx) {
+  CKL(scft::launch_free_energy_partials(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->M,
+                                        ctx->batch, ctx->partial, ctx->nblk, ctx->st));
+  CKL(scft::launch_free_energy_finalize(ctx->partial, ctx->nblk, ctx->batch, ctx->M, ctx->Q,
+                                        ctx->fe5, ctx->st));
+  return SCFT_OK;
+}
+
+int read_fe(scft_ctx *ctx, double *out5) {
+  CK(cudaMemcpyAsync(out5, ctx->fe5, sizeof(double) * 5 * ctx->batch, cudaMemcpyDeviceToHost,
+                     ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  for (int i = 0; i < 5 * ctx->batch; ++i)
+    if (!isfinite(out5[i])) return scft_fail(ctx, SCFT_ERR_NOT_FINITE, "free energy is not finite");
+  return SCFT_OK;
+}
+
+int iterate_once(scft_ctx *ctx) {
+  int rc;
+  if ((rc = average(ctx, ctx->wa))) return rc;   // cuda_scft.cu:170
+  if ((rc = average(ctx, ctx->wb))) return rc;   // :172
+  if ((rc = get_conc(ctx))) return rc;           // :174
+  return mix(ctx);                               // :182
+}
+
+void free_all(scft_ctx *ctx) {
+  cudaFree(ctx->wa); cudaFree(ctx->wb); cudaFree(ctx->pha); cudaFree(ctx->phb);
+  for (int i = 0; i < 4; ++i) cudaFree(ctx->q[i]);
+  cudaFree(ctx->qint); cudaFree(ctx->W); cudaFree(ctx->tmp[0]); cudaFree(ctx->tmp[1]);
+  cudaFree(ctx->partial); cudaFree(ctx->sum); cudaFree(ctx->Q); cudaFree(ctx->ffl);
+  cudaFree(ctx->fe5); cudaFree(ctx->tables);
+  for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
+  ctx->prof_events.clear();
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+}
+
+}  // namespace
+
+int scft_fail(scft_ctx *ctx, int status, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  else g_create_err = msg;
+  return status;
+}
+
+extern "C" {
+
+int scft_params_default(scft_params *p) {
+  if (!p) return SCFT_ERR_INVALID_ARG;
+  memset(p, 0, sizeof(*p));
+  p->nx = p->ny = p->nz = 32;
+  p->lx = p->ly = p->lz = 4.0;
+  p->hAB = 20.0;
+  p->fA = 0.5;
+  p->ds0 = 0.01;
+  p->batch = 1;
+  p->precision = SCFT_PREC_FP64;
+  p->wopt = 0.05;
+  p->wcmp = 0.10;
+  p->mixing = SCFT_MIX_SIMPLE;
+  p->anderson_history = 20;
+  p->anderson_lambda = 0.1;
+  p->device = 0;
+  return SCFT_OK;
+}
+
+int scft_grid_supported(int nx, int ny, int nz) {
+  return axis_ok(nx, false) && axis_ok(ny, true) && axis_ok(nz, true);
+}
+
+const char *scft_strerror(int s) {
+  switch (s) {
+    case SCFT_OK: return "ok";
+    case SCFT_ERR_INVALID_ARG: return "invalid argument";
+    case SCFT_ERR_UNSUPPORTED: return "unsupported grid or option";
+    case SCFT_ERR_CUDA: return "CUDA error";
+    case SCFT_ERR_NO_MEMORY: return "out of memory";
+    case SCFT_ERR_NOT_FINITE: return "non-finite value";
+    case SCFT_ERR_IO: return "I/O error";
+    case SCFT_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char *scft_last_error(const scft_ctx *ctx) {
+  return ctx ? ctx->err.c_str() : g_create_err.c_str();
+}
+
+int scft_create(const scft_params *pin, scft_ctx **out) {
+  scft_ctx *ctx = nullptr;
+  if (!pin || !out) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  const scft_params &p = *pin;
+  for (int i = 0; i < 8; ++i)
+    if (p.reserved[i]) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "reserved fields must be 0");
+  if (!(p.lx > 0 && p.ly > 0 && p.lz > 0 && p.ds0 > 0 && p.fA >= 0 && p.fA <= 1 && p.batch >= 1))
+    return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
+  if (p.precision != SCFT_PREC_FP64 && p.precision != SCFT_PREC_FP32)
+    return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad precision");
+  if (p.mixing != SCFT_MIX_SIMPLE)
+    return scft_fail(nullptr, SCFT_ERR_UNSUPPORTED, "only simple mixing is available");
+  if (!scft_grid_supported(p.nx, p.ny, p.nz))
+    return scft_fail(nullptr, SCFT_ERR_UNSUPPORTED,
+                     "grid unsupported: Nx must be even, Ny/Nz even or 1, each <= 4096 with "
+                     "prime factors <= 61");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return scft_fail(nullptr, SCFT_ERR_NO_DEVICE, "no CUDA device");
+  if (p.device < 0 || p.device >= ndev)
+    return scft_fail(nullptr, SCFT_ERR_NO_DEVICE, "bad device ordinal");
+  if (cudaSetDevice(p.device) != cudaSuccess)
+    return scft_fail(nullptr, SCFT_ERR_NO_DEVICE, "cudaSetDevice failed");
+
+  ctx = new scft_ctx();
+  ctx->p = p;
+  ctx->M = (long long)p.nx * p.ny * p.nz;
+  ctx->batch = p.batch;
+  ctx->rbytes = p.precision == SCFT_PREC_FP32 ? 4 : 8;
+  ctx->NsA = (int)(p.fA / p.ds0 + 1.0e-8);            // init_cuda.cu:330
+  ctx->dNsB = (int)((1 - p.fA) / p.ds0 + 1.0e-8);     // init_cuda.cu:329,331
+  ctx->q_ns[SCFT_Q_A] = ctx->q_ns[SCFT_Q_CA] = ctx->NsA;
+  ctx->q_ns[SCFT_Q_B] = ctx->q_ns[SCFT_Q_CB] = ctx->dNsB;
+  const long long M = ctx->M, B = ctx->batch;
+  const size_t rb = ctx->rbytes;
+
+  auto fail = [&](int st, const std::string &m) {
+    std::string msg = m;
+    free_all(ctx);
+    delete ctx;
+    return scft_fail(nullptr, st, msg);
+  };
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(SCFT_ERR_CUDA, "stream creation failed");
+  if (scft::line_filter_prepare() != cudaSuccess)
+    return fail(SCFT_ERR_CUDA, "kernel attribute set-up failed");
+
+  auto alloc = [&](void **ptr, size_t bytes) {
+    if (cudaMalloc(ptr, bytes) != cudaSuccess) { *ptr = nullptr; return false; }
+    return cudaMemset(*ptr, 0, bytes) == cudaSuccess;
+  };
+  bool ok = alloc((void **)&ctx->wa, 8 * M * B) && alloc((void **)&ctx->wb, 8 * M * B) &&
+            alloc((void **)&ctx->pha, 8 * M * B) && alloc((void **)&ctx->phb, 8 * M * B);
+  for (int i = 0; ok && i < 4; ++i) ok = alloc(&ctx->q[i], rb * M * B * (ctx->q_ns[i] + 1));
+  ok = ok && alloc(&ctx->qint, rb * M * B) && alloc(&ctx->W, rb * M * B) &&
+       alloc(&ctx->tmp[0], rb * M * B) && alloc(&ctx->tmp[1], rb * M * B);
+  ctx->nblk = scft::reduce_blocks(M);
+  ok = ok && alloc((void **)&ctx->partial, 8 * B * 3 * ctx->nblk) &&
+       alloc((void **)&ctx->sum, 8 * B) && alloc((void **)&ctx->Q, 8 * B) &&
+       alloc((void **)&ctx->ffl, 8 * B) && alloc((void **)&ctx->fe5, 8 * 5 * B);
+  if (!ok) {
+    cudaGetLastError();
+    return fail(SCFT_ERR_NO_MEMORY, "device allocation failed");
+  }
+
+  // ---- per-axis spectral tables (init_cuda.cu:394-428, split per axis)
+  const int dims[3] = {p.nx, p.ny, p.nz};
+  const double lens[3] = {p.lx, p.ly, p.lz};
+  double scalar = 1.0;  // gains of length-1 axes, folded into the first pass
+  std::vector<int> axes;
+  for (int a = 0; a < 3; ++a) {
+    if (dims[a] == 1) scalar *= exp(-p.ds0 * k2_axis(1, lens[a])[0]);
+    else axes.push_back(a);
+  }
+  size_t tab_bytes = 0;
+  for (int a : axes) tab_bytes += (size_t)dims[a] * 3 * rb + 256;
+  if (!alloc(&ctx->tables, tab_bytes)) return fail(SCFT_ERR_NO_MEMORY, "table allocation failed");
+  std::vector<unsigned char> host(tab_bytes, 0);
+  size_t off = 0;
+  for (size_t ai = 0; ai < axes.size(); ++ai) {
+    const int a = axes[ai];
+    const int n = dims[a];
+    AxisPlan ap;
+    memset(&ap, 0, sizeof(ap));
+    ap.n = n;
+    radix_plan(n, ap.fac, &ap.nfac);
+    if (a == 0) {        // x: rows of Nx, contiguous
+      ap.s_n = 1; ap.s_pair = p.nx; ap.s_outer = 0; ap.n_real = p.ny * p.nz; ap.n_outer = 1;
+      ap.n_fast = 1;
+    } else if (a == 1) { // y: stride Nx, pairs along x, outer z
+      ap.s_n = p.nx; ap.s_pair = 1; ap.s_outer = (long long)p.nx * p.ny; ap.n_real = p.nx;
+      ap.n_outer = p.nz; ap.n_fast = 0;
+    } else {             // z: stride Nx*Ny, pairs along x, outer y
+      ap.s_n = (long long)p.nx * p.ny; ap.s_pair = 1; ap.s_outer = p.nx; ap.n_real = p.nx;
+      ap.n_outer = p.ny; ap.n_fast = 0;
+    }
+    const int n_pairs = (ap.n_real + 1) / 2;
+    int tl = (int)(65536 / (4 * (size_t)n * rb));
+    if (tl > 32) tl = 32;
+    if (tl < 1) tl = 1;
+    if (tl > n_pairs) tl = n_pairs;
+    ap.tl = tl;
+    if (scft::line_filter_smem_bytes(ap, rb) > (size_t)scft::kLineSmemMax)
+      return fail(SCFT_ERR_UNSUPPORTED, "line too long for shared memory");
+    // twiddles exp(-2 pi i m / n) and gains exp(-ds0 k^2)/n
+    const std::vector<double> k2 = k2_axis(n, lens[a]);
+    const size_t tw_off = off, g_off = off + (size_t)n * 2 * rb;
+    for (int m = 0; m < n; ++m) {
+      const double ang = -2.0 * M_PI * (double)m / (double)n;
+      const double c = cos(ang), s = sin(ang);
+      double g = exp(-p.ds0 * k2[m]) / n;
+      if (ai == 0) g *= scalar;
+      if (rb == 4) {
+        float *t = reinterpret_cast<float *>(&host[tw_off]);
+        t[2 * m] = (float)c; t[2 * m + 1] = (float)s;
+        reinterpret_cast<float *>(&host[g_off])[m] = (float)g;
+      } else {
+        double *t = reinterpret_cast<double *>(&host[tw_off]);
+        t[2 * m] = c; t[2 * m + 1] = s;
+        reinterpret_cast<double *>(&host[g_off])[m] = g;
+      }
+    }
+    ap.twiddle = static_cast<unsigned char *>(ctx->tables) + tw_off;
+    ap.gain = static_cast<unsigned char *>(ctx->tables) + g_off;
+    off += (size_t)n * 3 * rb;
+    off = (off + 255) & ~(size_t)255;
+    ctx->passes.push_back(ap);
+  }
+  if (cudaMemcpy(ctx->tables, host.data(), tab_bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(SCFT_ERR_CUDA, "table upload failed");
+  if (cudaDeviceSynchronize() != cudaSuccess) return fail(SCFT_ERR_CUDA, "set-up failed");
+  ctx->err = "no error";
+  *out = ctx;
+  return SCFT_OK;
+}
+
+void scft_destroy(scft_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->p.device);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  free_all(ctx);
+  delete ctx;
+}
+
+int scft_get_ns(const scft_ctx *ctx, int *NsA, int *dNsB) {
+  if (!ctx || !NsA || !dNsB) return SCFT_ERR_INVALID_ARG;
+  *NsA = ctx->NsA;
+  *dNsB = ctx->dNsB;
+  return SCFT_OK;
+}
+
+static double *field_ptr(scft_ctx *ctx, int f) {
+  switch (f) {
+    case SCFT_FIELD_WA: return ctx->wa;
+    case SCFT_FIELD_WB: return ctx->wb;
+    case SCFT_FIELD_PHA: return ctx->pha;
+    case SCFT_FIELD_PHB: return ctx->phb;
+    default: return nullptr;
+  }
+}
+
+int scft_set_field(scft_ctx *ctx, int field, const double *src) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  double *d = field_ptr(ctx, field);
+  if (!d || !src) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad field or null pointer");
+  CK(cudaMemcpyAsync(d, src, sizeof(double) * ctx->M * ctx->batch, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return SCFT_OK;
+}
+
+int scft_get_field(scft_ctx *ctx, int field, double *dst) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  double *d = field_ptr(ctx, field);
+  if (!d || !dst) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad field or null pointer");
+  CK(cudaMemcpyAsync(dst, d, sizeof(double) * ctx->M * ctx->batch, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return SCFT_OK;
+}
+
+int scft_average_value(scft_ctx *ctx, int field) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  if (field != SCFT_FIELD_WA && field != SCFT_FIELD_WB)
+    return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "average_value applies to wa or wb");
+  return average(ctx, field_ptr(ctx, field));
+}
+
+int scft_sov_dif_fft(scft_ctx *ctx, int q, int w_field, int ns, int sign) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  if (q < 0 || q > 3 || (w_field != SCFT_FIELD_WA && w_field != SCFT_FIELD_WB) ||
+      (sign != 1 && sign != -1) || ns < 0 || ns > ctx->q_ns[q])
+    return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad propagator, field, sign or ns");
+  return march(ctx, q, w_field, ns, sign);
+}
+
+int scft_set_qint(scft_ctx *ctx, int q, int s) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  if (q > 3 || (q >= 0 && (s < 0 || s > ctx->q_ns[q])))
+    return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad propagator or slice");
+  return set_qint(ctx, q, s);
+}
+
+int scft_get_q(scft_ctx *ctx, int q, int s, double *dst) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  if (q < 0 || q > 3 || s < 0 || s > ctx->q_ns[q] || !dst)
+    return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad propagator, slice or pointer");
+  const long long M = ctx->M;
+  const long long qbs = (long long)(ctx->q_ns[q] + 1) * M;
+  // stage through the (FP64-sized) phi scratch: cast on the device, then copy
+  double *stage = nullptr;
+  CK(cudaMallocAsync((void **)&stage, sizeof(double) * M * ctx->batch, ctx->st));
+  if (ctx->rbytes == 4)
+    CKL(scft::launch_cast_slice<float>(stage, M, static_cast<float *>(ctx->q[q]) + (long long)s * M,
+                                       qbs, M, ctx->batch, ctx->st));
+  else
+    CKL(scft::launch_cast_slice<double>(stage, M, static_cast<double *>(ctx->q[q]) + (long long)s * M,
+                                        qbs, M, ctx->batch, ctx->st));
+  CK(cudaMemcpyAsync(dst, stage, sizeof(double) * M * ctx->batch, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaFreeAsync(stage, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return SCFT_OK;
+}
+
+int scft_get_conc(scft_ctx *ctx) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  return get_conc(ctx);
+}
+
+int scft_get_Q(scft_ctx *ctx, double *dst) {
+  if (!ctx || !dst) return SCFT_ERR_INVALID_ARG;
+  CK(cudaMemcpyAsync(dst, ctx->Q, sizeof(double) * ctx->batch, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return SCFT_OK;
+}
+
+int scft_phi_w(scft_ctx *ctx) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  return mix(ctx);
+}
+
+int scft_free_energy(scft_ctx *ctx, double *out5) {
+  if (!ctx || !out5) return SCFT_ERR_INVALID_ARG;
+  int rc = free_energy_dev(ctx);
+  if (rc) return rc;
+  return read_fe(ctx, out5);
+}
+
+int scft_iterate(scft_ctx *ctx, int n_iter, double *out5) {
+  if (!ctx || n_iter < 0) return SCFT_ERR_INVALID_ARG;
+  for (int it = 0; it < n_iter; ++it) {
+    int rc = iterate_once(ctx);
+    if (rc) return rc;
+  }
+  if (out5) {
+    int rc = free_energy_dev(ctx);
+    if (rc) return rc;
+    return read_fe(ctx, out5);
+  }
+  return SCFT_OK;
+}
+
+int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir) {
+  if (!ctx || max_it < 0 || aver_it < 1) return SCFT_ERR_INVALID_ARG;
+  std::vector<double> fe(5 * ctx->batch);
+  int iter = 0;
+  do {                                   // cuda_scft.cu:167-253
+    iter = iter + 1;
+    int rc = iterate_once(ctx);
+    if (rc) return rc;
+    if (iter % aver_it == 0) {
+      if ((rc = free_energy_dev(ctx))) return rc;
+      if ((rc = read_fe(ctx, fe.data()))) return rc;
+      for (int i = 0; i < ctx->batch; ++i)
+        printf("GPU %d batch %d: %5d : %.8e, %.8e, %.8e,%.8e, %.8e\n", 0, i, iter, fe[5 * i + 0],
+               fe[5 * i + 1], fe[5 * i + 2], fe[5 * i + 3], fe[5 * i + 4]);
+      fflush(stdout);
+      if (outdir && iter % (aver_it * 10) == 0) {
+        for (int i = 0; i < ctx->batch; ++i) {
+          std::string path = std::string(outdir) + "/pha_" + std::to_string(i + 1) + ".dat";
+          if ((rc = scft_write_pha_dat(ctx, path.c_str(), i))) return rc;
+        }
+      }
+    }
+  } while (iter < max_it);
+  return SCFT_OK;
+}
+
+int scft_synchronize(scft_ctx *ctx) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  CK(cudaStreamSynchronize(ctx->st));
+  return SCFT_OK;
+}
+
+long long scft_launch_count(const scft_ctx *ctx) { return ctx ? ctx->launches : -1; }
+
+int scft_time_iterations(scft_ctx *ctx, int n_iter, double *ms) {
+  if (!ctx || !ms || n_iter < 0) return SCFT_ERR_INVALID_ARG;
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaEventRecord(a, ctx->st));
+  int rc = SCFT_OK;
+  for (int it = 0; it < n_iter && rc == SCFT_OK; ++it) rc = iterate_once(ctx);
+  cudaEventRecord(b, ctx->st);
+  cudaEventSynchronize(b);
+  float f = 0.f;
+  cudaEventElapsedTime(&f, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = f;
+  return rc;
+}
+
+int scft_profile_enable(scft_ctx *ctx, int enable) {
+  if (!ctx || enable < 0) return SCFT_ERR_INVALID_ARG;
+  ctx->profiling = enable > 0;
+  if (enable > 0) return prof_reserve(ctx, 2 * (size_t)enable);
+  return SCFT_OK;
+}
+
+int scft_profile_read(scft_ctx *ctx, double *march_ms, long long *n_marches,
+                      double *point_steps) {
+  if (!ctx || !march_ms || !n_marches || !point_steps) return SCFT_ERR_INVALID_ARG;
+  CK(cudaStreamSynchronize(ctx->st));
+  double tot = 0.0;
+  for (size_t i = 0; i + 1 < ctx->prof_used; i += 2) {
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, ctx->prof_events[i], ctx->prof_events[i + 1]));
+    tot += f;
+  }
+  *march_ms = tot;
+  *n_marches = (long long)(ctx->prof_used / 2);
+  *point_steps = ctx->prof_point_steps;
+  ctx->prof_used = 0;
+  ctx->prof_point_steps = 0.0;
+  return SCFT_OK;
+}
+
+}  // extern "C"

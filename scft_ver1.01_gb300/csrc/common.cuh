@@ -1,0 +1,59 @@
+// Shared device/host helpers for the SCFT GB300 kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace scft {
+
+// Complex type matched to the working real type.
+template <typename R> struct cplx;
+template <> struct cplx<float> { typedef float2 type; };
+template <> struct cplx<double> { typedef double2 type; };
+
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  C r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) {
+  C r; r.x = a.x + b.x; r.y = a.y + b.y; return r;
+}
+template <typename C> __device__ __forceinline__ C csub(C a, C b) {
+  C r; r.x = a.x - b.x; r.y = a.y - b.y; return r;
+}
+// multiply by -i
+template <typename C> __device__ __forceinline__ C cmul_mi(C a) {
+  C r; r.x = a.y; r.y = -a.x; return r;
+}
+template <typename C, typename R> __device__ __forceinline__ C cscale(C a, R s) {
+  C r; r.x = a.x * s; r.y = a.y * s; return r;
+}
+template <typename C> __device__ __forceinline__ C cconj(C a) {
+  C r; r.x = a.x; r.y = -a.y; return r;
+}
+template <typename C, typename R> __device__ __forceinline__ C mkc(R x, R y) {
+  C r; r.x = x; r.y = y; return r;
+}
+
+// Warp-level sum of a double.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Error-free transformation a+b = s+e (Knuth TwoSum), FP32.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+}  // namespace scft

@@ -1,0 +1,45 @@
+// Internal state behind the opaque scft_ctx of include/scft_capi.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/scft_capi.h"
+#include "kernels.h"
+
+struct scft_ctx {
+  scft_params p;
+  int NsA = 0, dNsB = 0;
+  long long M = 0;
+  int batch = 0;
+  int rbytes = 8;               // sizeof working real (4 or 8)
+  cudaStream_t st = nullptr;
+  std::string err;
+  long long launches = 0;
+
+  // FP64 fields [batch][M]
+  double *wa = nullptr, *wb = nullptr, *pha = nullptr, *phb = nullptr;
+  // propagators [batch][ns_q+1][M] in the working precision
+  void *q[4] = {nullptr, nullptr, nullptr, nullptr};
+  int q_ns[4] = {0, 0, 0, 0};
+  void *qint = nullptr;         // [batch][M]
+  void *W = nullptr;            // Boltzmann factor [batch][M]
+  void *tmp[2] = {nullptr, nullptr};
+  // reductions
+  int nblk = 1;
+  double *partial = nullptr;    // [batch][3][nblk]
+  double *sum = nullptr, *Q = nullptr, *ffl = nullptr, *fe5 = nullptr;
+  // spectral tables (twiddles + gains of each pass), device
+  void *tables = nullptr;
+  std::vector<scft::AxisPlan> passes;
+  // per-march event timing
+  bool profiling = false;
+  std::vector<cudaEvent_t> prof_events;   // pairs, grown on demand
+  size_t prof_used = 0;
+  double prof_point_steps = 0.0;
+};
+
+// Set ctx->err and return status.
+int scft_fail(scft_ctx *ctx, int status, const std::string &msg);

@@ -1,0 +1,322 @@
+// Field kernels of the SCF iteration: Boltzmann factors, propagator
+// hand-offs, deterministic per-instance reductions (mean subtraction, Q, free
+// energy), the trapezoid contour sum giving phi, and simple mixing.
+// All reductions are two-level and in a fixed order, so results are
+// bit-reproducible from run to run.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace scft {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;  // valid in thread 0
+}
+__device__ __forceinline__ double block_max(double v, double *sh) {
+  v = warp_max(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    r = warp_max(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+template <typename R>
+__global__ void k_boltzmann(const double *__restrict__ w, R *__restrict__ W, long long n,
+                            double ds2) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    W[i] = (R)exp(-w[i] * ds2);   // initilize_wdz, cuda_aid.cu:254
+}
+
+template <typename R>
+__global__ void k_fill(R *__restrict__ x, long long n, R v, long long bs) {
+  R *xb = x + blockIdx.y * bs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    xb[i] = v;
+}
+
+template <typename R, typename D>
+__global__ void k_copy(D *__restrict__ dst, long long dbs, const R *__restrict__ src,
+                       long long sbs, long long M) {
+  D *d = dst + blockIdx.y * dbs;
+  const R *s = src + blockIdx.y * sbs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x)
+    d[i] = (D)s[i];
+}
+
+template <typename R>
+__global__ void k_partial_sum(const R *__restrict__ x, long long bs, long long M,
+                              double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const R *xb = x + blockIdx.y * bs;
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x)
+    acc += (double)xb[i];
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = acc;
+}
+
+__global__ void k_finalize_sum(const double *__restrict__ partial, int nblk, double scale,
+                               double *__restrict__ out) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) acc += partial[blockIdx.x * nblk + i];
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) out[blockIdx.x] = acc * scale;
+}
+
+__global__ void k_minus_average(double *__restrict__ data, const double *__restrict__ sum,
+                                long long M) {
+  double *d = data + blockIdx.y * M;
+  const double s = sum[blockIdx.y];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x)
+    d[i] = d[i] - s / (double)M;   // minus_average, cuda_aid.cu:377
+}
+
+__global__ void k_q_ffl(const double *__restrict__ sum, long long M, double ds0, int batch,
+                        double *__restrict__ Q, double *__restrict__ ffl) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch) {
+    const double q = sum[b] / (double)M;  // cuda_scft.cu:124
+    Q[b] = q;
+    ffl[b] = ds0 / q;                      // cuda_scft.cu:125
+  }
+}
+
+// Trapezoid contour sum (w_to_phi_go, cuda_aid.cu:87-112).  q, qc are
+// contour-outer [b][s][M].  FP64 accumulation for double; for float the
+// products are accumulated with a compensated (TwoSum) FP32 pair, which keeps
+// ~FP64-level summation error without GB300's slow FP64 pipe.
+template <typename R>
+__global__ void k_contour_phi(const R *__restrict__ q, const R *__restrict__ qc, int ns,
+                              long long M, const double *__restrict__ ffl,
+                              double *__restrict__ phi);
+
+template <>
+__global__ void k_contour_phi<double>(const double *__restrict__ q, const double *__restrict__ qc,
+                                      int ns, long long M, const double *__restrict__ ffl,
+                                      double *__restrict__ phi) {
+  const int b = blockIdx.y;
+  const long long qbs = (long long)(ns + 1) * M;
+  const double *qb = q + b * qbs, *qcb = qc + b * qbs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x) {
+    // ns == 0: the single end point gets weight 1/2 (cuda_aid.cu:91)
+    double acc = 0.5 * qb[i] * qcb[i];
+    for (int s = 1; s < ns; ++s) acc += qb[s * M + i] * qcb[s * M + i];
+    if (ns > 0) acc += 0.5 * qb[ns * M + i] * qcb[ns * M + i];
+    phi[b * M + i] = acc * ffl[b];
+  }
+}
+
+template <>
+__global__ void k_contour_phi<float>(const float *__restrict__ q, const float *__restrict__ qc,
+                                     int ns, long long M, const double *__restrict__ ffl,
+                                     double *__restrict__ phi) {
+  const int b = blockIdx.y;
+  const long long qbs = (long long)(ns + 1) * M;
+  const float *qb = q + b * qbs, *qcb = qc + b * qbs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x) {
+    float hi = 0.f, lo = 0.f;
+    for (int s = 1; s < ns; ++s) {
+      const float p = qb[s * M + i] * qcb[s * M + i];
+      float e;
+      two_sum(hi, p, hi, e);
+      lo += e;
+    }
+    const double ends = ns > 0 ? 0.5 * ((double)qb[i] * qcb[i] + (double)qb[ns * M + i] * qcb[ns * M + i])
+                               : 0.5 * (double)qb[i] * qcb[i];
+    phi[b * M + i] = ((double)hi + (double)lo + ends) * ffl[b];
+  }
+}
+
+__global__ void k_phi_w(double *__restrict__ wa, double *__restrict__ wb,
+                        const double *__restrict__ pha, const double *__restrict__ phb,
+                        double hAB, double wopt, double wcmp, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    // phi_w, cuda_aid.cu:398-412
+    const double a = wa[i], b = wb[i], pa = pha[i], pb = phb[i];
+    const double eta = (a + b - hAB) / 2;
+    const double psum = 1.0 - pa - pb;
+    double da = hAB * pb + eta - a;
+    double db = hAB * pa + eta - b;
+    da -= wcmp * psum;
+    db -= wcmp * psum;
+    wa[i] = a + wopt * da;
+    wb[i] = b + wopt * db;
+  }
+}
+
+// partial layout: [b][3][nblk]
+__global__ void k_fe_partials(const double *__restrict__ wa, const double *__restrict__ wb,
+                              const double *__restrict__ pha, const double *__restrict__ phb,
+                              double hAB, long long M, double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const long long o = blockIdx.y * M;
+  double fab = 0.0, fw = 0.0, inc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double pa = pha[o + i], pb = phb[o + i];
+    fab += hAB * pa * pb;                          // cuda_scft.cu:207
+    fw += wa[o + i] * pa + wb[o + i] * pb;         // cuda_scft.cu:208
+    inc = fmax(inc, fabs(1.0 - pa - pb));          // cuda_scft.cu:203-206
+  }
+  const int nb = gridDim.x;
+  double r;
+  r = block_sum(fab, sh);
+  if (threadIdx.x == 0) partial[(blockIdx.y * 3 + 0) * nb + blockIdx.x] = r;
+  r = block_sum(fw, sh);
+  if (threadIdx.x == 0) partial[(blockIdx.y * 3 + 1) * nb + blockIdx.x] = r;
+  r = block_max(inc, sh);
+  if (threadIdx.x == 0) partial[(blockIdx.y * 3 + 2) * nb + blockIdx.x] = r;
+}
+
+// out5[b] = {F, F_AB, F_W, F_S, inCompMax}
+__global__ void k_fe_finalize(const double *__restrict__ partial, int nblk, long long M,
+                              const double *__restrict__ Q, double *__restrict__ out5) {
+  __shared__ double sh[32];
+  const int b = blockIdx.x;
+  double s0 = 0.0, s1 = 0.0, m2 = 0.0;
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
+    s0 += partial[(b * 3 + 0) * nblk + i];
+    s1 += partial[(b * 3 + 1) * nblk + i];
+    m2 = fmax(m2, partial[(b * 3 + 2) * nblk + i]);
+  }
+  s0 = block_sum(s0, sh);
+  s1 = block_sum(s1, sh);
+  m2 = block_max(m2, sh);
+  if (threadIdx.x == 0) {
+    const double fab = s0 / (double)M, fw = -s1 / (double)M, fs = -log(Q[b]);
+    out5[b * 5 + 0] = fab + fw + fs;   // cuda_scft.cu:220
+    out5[b * 5 + 1] = fab;
+    out5[b * 5 + 2] = fw;
+    out5[b * 5 + 3] = fs;
+    out5[b * 5 + 4] = m2;
+  }
+}
+
+inline int grid_for(long long n) {
+  long long g = (n + kThreads - 1) / kThreads;
+  if (g > 152 * 16) g = 152 * 16;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+}  // namespace
+
+int reduce_blocks(long long M) {
+  long long g = (M + kThreads * 4 - 1) / (kThreads * 4);
+  if (g > 304) g = 304;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+template <typename R>
+cudaError_t launch_boltzmann(const double *w, R *W, long long n, double ds2, cudaStream_t st) {
+  k_boltzmann<R><<<grid_for(n), kThreads, 0, st>>>(w, W, n, ds2);
+  return cudaGetLastError();
+}
+template <typename R>
+cudaError_t launch_fill(R *x, long long n, R v, long long bstride, int batch, cudaStream_t st) {
+  k_fill<R><<<dim3(grid_for(n), batch), kThreads, 0, st>>>(x, n, v, bstride);
+  return cudaGetLastError();
+}
+template <typename R>
+cudaError_t launch_copy_slice(R *dst, long long dbs, const R *src, long long sbs, long long M,
+                              int batch, cudaStream_t st) {
+  k_copy<R, R><<<dim3(grid_for(M), batch), kThreads, 0, st>>>(dst, dbs, src, sbs, M);
+  return cudaGetLastError();
+}
+template <typename R>
+cudaError_t launch_cast_slice(double *dst, long long dbs, const R *src, long long sbs,
+                              long long M, int batch, cudaStream_t st) {
+  k_copy<R, double><<<dim3(grid_for(M), batch), kThreads, 0, st>>>(dst, dbs, src, sbs, M);
+  return cudaGetLastError();
+}
+template <typename R>
+cudaError_t launch_partial_sum(const R *x, long long bs, long long M, int batch, double *partial,
+                               int nblk, cudaStream_t st) {
+  k_partial_sum<R><<<dim3(nblk, batch), kThreads, 0, st>>>(x, bs, M, partial);
+  return cudaGetLastError();
+}
+cudaError_t launch_finalize_sum(const double *partial, int nblk, int batch, double scale,
+                                double *out, cudaStream_t st) {
+  k_finalize_sum<<<batch, kThreads, 0, st>>>(partial, nblk, scale, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_minus_average(double *data, const double *sum, long long M, int batch,
+                                 cudaStream_t st) {
+  k_minus_average<<<dim3(grid_for(M), batch), kThreads, 0, st>>>(data, sum, M);
+  return cudaGetLastError();
+}
+cudaError_t launch_q_ffl(const double *sum, long long M, double ds0, int batch, double *Q,
+                         double *ffl, cudaStream_t st) {
+  k_q_ffl<<<(batch + 127) / 128, 128, 0, st>>>(sum, M, ds0, batch, Q, ffl);
+  return cudaGetLastError();
+}
+template <typename R>
+cudaError_t launch_contour_phi(const R *q, const R *qc, int ns, long long M, int batch,
+                               const double *ffl, double *phi, cudaStream_t st) {
+  k_contour_phi<R><<<dim3(grid_for(M), batch), kThreads, 0, st>>>(q, qc, ns, M, ffl, phi);
+  return cudaGetLastError();
+}
+cudaError_t launch_phi_w(double *wa, double *wb, const double *pha, const double *phb,
+                         double hAB, double wopt, double wcmp, long long M, int batch,
+                         cudaStream_t st) {
+  const long long n = M * batch;
+  k_phi_w<<<grid_for(n), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, wopt, wcmp, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_free_energy_partials(const double *wa, const double *wb, const double *pha,
+                                        const double *phb, double hAB, long long M, int batch,
+                                        double *partial, int nblk, cudaStream_t st) {
+  k_fe_partials<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, M, partial);
+  return cudaGetLastError();
+}
+cudaError_t launch_free_energy_finalize(const double *partial, int nblk, int batch, long long M,
+                                        const double *Q, double *out5, cudaStream_t st) {
+  k_fe_finalize<<<batch, kThreads, 0, st>>>(partial, nblk, M, Q, out5);
+  return cudaGetLastError();
+}
+
+#define INST(R)                                                                                  \
+  template cudaError_t launch_boltzmann<R>(const double *, R *, long long, double, cudaStream_t); \
+  template cudaError_t launch_fill<R>(R *, long long, R, long long, int, cudaStream_t);           \
+  template cudaError_t launch_copy_slice<R>(R *, long long, const R *, long long, long long, int, \
+                                            cudaStream_t);                                        \
+  template cudaError_t launch_cast_slice<R>(double *, long long, const R *, long long, long long, \
+                                            int, cudaStream_t);                                   \
+  template cudaError_t launch_partial_sum<R>(const R *, long long, long long, int, double *, int, \
+                                             cudaStream_t);                                       \
+  template cudaError_t launch_contour_phi<R>(const R *, const R *, int, long long, int,           \
+                                             const double *, double *, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace scft

@@ -1,0 +1,83 @@
+// Host-side launchers of the SCFT kernels (all run on one CUDA stream each).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace scft {
+
+// One per-axis pass of the separable diffusion operator exp(-k^2 ds):
+// every line along the axis is transformed, multiplied by the real, even
+// gain g[k] (= exp(-ds*k^2)/N, the reference's kxyzdz factor split per axis),
+// and transformed back.  Two real lines are packed as the real and imaginary
+// parts of one complex line; because g is real and even the two lines do not
+// mix.  Geometry of the real lines of one instance:
+//   element (outer o, real line r, position n) at  o*s_outer + r*s_pair + n*s_n
+struct AxisPlan {
+  int n;                 // line length
+  int nfac;              // radix plan (Stockham stages), product == n
+  int fac[24];
+  long long s_n, s_pair, s_outer;
+  int n_real;            // real lines per outer group (paired 2 by 2)
+  int n_outer;           // outer groups per instance
+  int n_fast;            // 1: consecutive threads walk n (contiguous lines)
+  int tl;                // complex lines per CTA tile
+  const void *twiddle;   // device: n complex, exp(-2*pi*i*m/n), working precision
+  const void *gain;      // device: n reals, working precision
+};
+
+// Generic mixed-radix Stockham line filter (any n whose prime factors are
+// <= 61).  in/out may not alias.  pre multiplies the input, post the output
+// (elementwise, indexed like one instance's grid); either may be null.
+template <typename R>
+cudaError_t launch_line_filter(const AxisPlan &ap, const R *in, long long in_bstride, R *out,
+                               long long out_bstride, const R *pre, const R *post,
+                               long long w_bstride, int batch, cudaStream_t st);
+
+size_t line_filter_smem_bytes(const AxisPlan &ap, size_t real_bytes);
+constexpr int kLineSmemMax = 200 * 1024;
+cudaError_t line_filter_prepare();
+
+// ---- field kernels (k_fields.cu) ----
+// W = exp(-w*ds2) in precision R, for batch*M points (w is FP64).
+template <typename R>
+cudaError_t launch_boltzmann(const double *w, R *W, long long n, double ds2, cudaStream_t st);
+template <typename R>
+cudaError_t launch_fill(R *x, long long n, R v, long long bstride, int batch, cudaStream_t st);
+// dst[b*dst_bstride + i] = src[b*src_bstride + i], i < M
+template <typename R>
+cudaError_t launch_copy_slice(R *dst, long long dst_bstride, const R *src, long long src_bstride,
+                              long long M, int batch, cudaStream_t st);
+template <typename R>
+cudaError_t launch_cast_slice(double *dst, long long dst_bstride, const R *src,
+                              long long src_bstride, long long M, int batch, cudaStream_t st);
+
+// Deterministic per-instance sums: partial[b*nblk+k] then finalize.
+int reduce_blocks(long long M);
+template <typename R>
+cudaError_t launch_partial_sum(const R *x, long long bstride, long long M, int batch,
+                               double *partial, int nblk, cudaStream_t st);
+cudaError_t launch_finalize_sum(const double *partial, int nblk, int batch, double scale,
+                                double *out, cudaStream_t st);
+// data -= sum/M  (minus_average)
+cudaError_t launch_minus_average(double *data, const double *sum, long long M, int batch,
+                                 cudaStream_t st);
+// Q = sum/M ; ffl = ds0/Q  (cal_ql + host lines of getConc)
+cudaError_t launch_q_ffl(const double *sum, long long M, double ds0, int batch, double *Q,
+                         double *ffl, cudaStream_t st);
+// phi = ffl * trapezoid contour sum of q*qc  (w_to_phi_go)
+template <typename R>
+cudaError_t launch_contour_phi(const R *q, const R *qc, int ns, long long M, int batch,
+                               const double *ffl, double *phi, cudaStream_t st);
+// simple mixing (phi_w); writes the residual max-norm partials if resid != null
+cudaError_t launch_phi_w(double *wa, double *wb, const double *pha, const double *phb,
+                         double hAB, double wopt, double wcmp, long long M, int batch,
+                         cudaStream_t st);
+// free energy partials: sums of hAB*pa*pb, wa*pa+wb*pb and max|1-pa-pb|
+cudaError_t launch_free_energy_partials(const double *wa, const double *wb, const double *pha,
+                                        const double *phb, double hAB, long long M, int batch,
+                                        double *partial, int nblk, cudaStream_t st);
+cudaError_t launch_free_energy_finalize(const double *partial, int nblk, int batch, long long M,
+                                        const double *Q, double *out5, cudaStream_t st);
+
+}  // namespace scft

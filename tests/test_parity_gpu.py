@@ -1,0 +1,223 @@
+"""GPU parity of the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances: the FP64 plain path must match the oracle to 1e-11 relative
+(rounding-level: the oracle uses pocketfft, the kernels a hand-written
+Stockham FFT); the FP32-propagation path to 2e-5 relative on propagators and
+phi (single-precision FFT round-off accumulated over the contour)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = {0: 1e-11, 1: 2e-5}
+
+GRIDS = [
+    (8, 8, 8, 3.0, 3.0, 3.0),
+    (16, 12, 8, 4.0, 3.0, 2.5),
+    (32, 32, 32, 4.0, 4.0, 4.0),
+    (48, 48, 48, 3.8, 3.8, 3.8),      # radix 3
+    (24, 20, 18, 3.0, 3.3, 2.7),      # radix 3 and 5
+    (16, 16, 1, 4.0, 4.0, 2.0),       # 2D, Nz=1 constant-factor quirk
+    (20, 1, 10, 3.0, 1.0, 2.0),       # Ny=1
+]
+
+
+def make_ctx(pkg, g, prec, batch=2, **kw):
+    nx, ny, nz, lx, ly, lz = g
+    return pkg.Context(nx=nx, ny=ny, nz=nz, lx=lx, ly=ly, lz=lz, batch=batch, precision=prec, **kw)
+
+
+def oparams(orc, g, batch=2, **kw):
+    nx, ny, nz, lx, ly, lz = g
+    return orc.Params(nx=nx, ny=ny, nz=nz, lx=lx, ly=ly, lz=lz, batch=batch, **kw)
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("g", GRIDS)
+def test_march_parity(pkg, orc, g, prec):
+    from scft_gb300 import fields
+    kw = dict(hAB=18.0, fA=0.36, ds0=0.02)
+    p = oparams(orc, g, **kw)
+    wa, wb = fields.gyroid(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 18.0, seed=1, batch=2)
+    with make_ctx(pkg, g, prec, **kw) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.set_qint(-1)
+        ctx.sov_dif_fft(pkg.Q_A, pkg.FIELD_WA, ctx.NsA, +1)
+        ctx.sov_dif_fft(pkg.Q_CB, pkg.FIELD_WB, ctx.dNsB, -1)
+        ref_a = orc.sov_dif_fft(np.ones_like(wa), wa, p.NsA, +1, p)
+        ref_cb = orc.sov_dif_fft(np.ones_like(wb), wb, p.dNsB, -1, p)
+        for s in (0, 1, p.NsA // 2, p.NsA):
+            assert rel(ctx.get_q(pkg.Q_A, s), ref_a[:, s]) < TOL[prec], s
+        for s in (0, p.dNsB - 1, p.dNsB // 3):
+            assert rel(ctx.get_q(pkg.Q_CB, s), ref_cb[:, s]) < TOL[prec], s
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("g", GRIDS[:5])
+def test_get_conc_parity(pkg, orc, g, prec):
+    from scft_gb300 import fields
+    kw = dict(hAB=20.0, fA=0.45, ds0=0.01)
+    p = oparams(orc, g, **kw)
+    wa, wb = fields.lamellar(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 20.0, seed=2, batch=2)
+    ref = orc.get_conc(wa, wb, p)
+    with make_ctx(pkg, g, prec, **kw) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.get_conc()
+        assert rel(ctx.pha, ref.pha) < TOL[prec]
+        assert rel(ctx.phb, ref.phb) < TOL[prec]
+        assert np.abs(ctx.Q() / ref.Q - 1).max() < TOL[prec]
+        assert rel(ctx.wa, ref.wa) < 1e-14           # getConc's own average_value
+        assert rel(ctx.get_q(pkg.Q_B, 0), ref.qb[:, 0]) < TOL[prec]
+        assert rel(ctx.get_q(pkg.Q_CA, p.NsA), ref.qca[:, p.NsA]) < TOL[prec]
+        assert rel(ctx.get_q(pkg.Q_CA, 0), ref.qca[:, 0]) < TOL[prec]
+
+
+def test_average_value_and_phi_w(pkg, orc):
+    g = GRIDS[1]
+    p = oparams(orc, g, hAB=15.0)
+    rng = np.random.default_rng(5)
+    wa, wb, pa, pb = rng.normal(0.5, 1, (4, 2) + p.shape)
+    with make_ctx(pkg, g, 0, hAB=15.0) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.average_value(pkg.FIELD_WA)
+        np.testing.assert_allclose(ctx.wa, orc.average_value(wa), rtol=0, atol=1e-14)
+        ctx.set_w(wa, wb)
+        ctx.set_field(pkg.FIELD_PHA, pa)
+        ctx.set_field(pkg.FIELD_PHB, pb)
+        ctx.phi_w()
+        ra, rb, _, _ = orc.phi_w(wa, wb, pa, pb, 15.0, 0.05, 0.10)
+        np.testing.assert_allclose(ctx.wa, ra, rtol=1e-15, atol=1e-14)
+        np.testing.assert_allclose(ctx.wb, rb, rtol=1e-15, atol=1e-14)
+        fe = ctx.free_energy()
+        Q = np.array([1.3, 0.7])
+        # free energy uses the device Q; set it through a conc evaluation instead
+        ctx.get_conc()
+        Qd = ctx.Q()
+        fe = ctx.free_energy()
+        F, fab, fw, fs, inc = orc.free_energy(ctx.wa, ctx.wb, ctx.pha, ctx.phb, Qd, 15.0)
+        np.testing.assert_allclose(fe[:, 0], F, rtol=1e-12)
+        np.testing.assert_allclose(fe[:, 1], fab, rtol=1e-12)
+        np.testing.assert_allclose(fe[:, 2], fw, rtol=1e-12)
+        np.testing.assert_allclose(fe[:, 3], fs, rtol=1e-12)
+        np.testing.assert_allclose(fe[:, 4], inc, rtol=1e-12)
+        del Q
+
+
+def test_free_loop_parity_fp64(pkg, orc, capfd):
+    # Free (cuda_scft.cu:140-269): 30 iterations, printed lines every 10
+    g = (16, 8, 8, 4.0, 2.0, 2.0)
+    kw = dict(hAB=20.0, fA=0.5, ds0=0.01)
+    p = oparams(orc, g, **kw)
+    from scft_gb300 import fields
+    wa, wb = fields.lamellar(16, 8, 8, 4.0, 2.0, 2.0, 20.0, seed=0, batch=2)
+    ref = orc.free_loop(wa, wb, p, 30)
+    with make_ctx(pkg, g, 0, **kw) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.free(30, 10)
+        out = capfd.readouterr().out.strip().splitlines()
+        assert rel(ctx.wa, ref.wa) < 1e-11
+        assert rel(ctx.wb, ref.wb) < 1e-11
+        assert rel(ctx.pha, ref.pha) < 1e-11
+    lines = [l for l in out if l.startswith("GPU ")]
+    assert len(lines) == 6
+    for l, row in zip(lines, ref.log):
+        it, b, F, fab, fw, fs, inc = row
+        vals = [float(v) for v in l.split(":")[2].split(",")]
+        assert l.startswith("GPU 0 batch %d: %5d :" % (b, it))
+        np.testing.assert_allclose(vals, [F, fab, fw, fs, inc], rtol=1e-7, atol=1e-12)
+
+
+def test_iterate_matches_free(pkg, orc):
+    g = (16, 8, 8, 4.0, 2.0, 2.0)
+    from scft_gb300 import fields
+    wa, wb = fields.lamellar(16, 8, 8, 4.0, 2.0, 2.0, 20.0, seed=0, batch=1)
+    p = oparams(orc, g, batch=1, hAB=20.0)
+    ref = orc.free_loop(wa, wb, p, 10)
+    with make_ctx(pkg, g, 0, batch=1, hAB=20.0) as ctx:
+        ctx.set_w(wa, wb)
+        fe = ctx.iterate(10, with_energy=True)
+    F, fab, fw, fs, inc = ref.log[-1][2:]
+    np.testing.assert_allclose(fe[0], [F, fab, fw, fs, inc], rtol=1e-10)
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (1, 2e-6)])
+def test_full_size_properties_128(pkg, prec, tol):
+    # 128^3, Ns=200: size-independent identities of the discretisation
+    from scft_gb300 import fields
+    n, L = 128, 3.8
+    with pkg.Context(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, hAB=18.0, fA=0.36, ds0=0.005,
+                     precision=prec) as ctx:
+        # zero field: Q == 1, phiA == NsA*ds, phiB == dNsB*ds
+        z = np.zeros(ctx.shape)
+        ctx.set_w(z, z)
+        ctx.get_conc()
+        assert abs(ctx.Q()[0] - 1) < tol
+        assert np.abs(ctx.pha - ctx.NsA * 0.005).max() < tol
+        # gyroid field: mean(phiA + phiB) == ds*(NsA + dNsB) (W D W is symmetric)
+        wa, wb = fields.gyroid(n, n, n, L, L, L, 18.0, seed=0)
+        ctx.set_w(wa, wb)
+        ctx.get_conc()
+        tot = (ctx.pha + ctx.phb).mean()
+        assert abs(tot - 0.005 * (ctx.NsA + ctx.dNsB)) < 5 * tol
+        assert np.isfinite(ctx.Q()).all()
+
+
+def test_full_size_fp32_vs_fp64_128(pkg):
+    from scft_gb300 import fields
+    n, L = 128, 3.8
+    wa, wb = fields.gyroid(n, n, n, L, L, L, 18.0, seed=0)
+    out = {}
+    for prec in (0, 1):
+        with pkg.Context(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, hAB=18.0, fA=0.36, ds0=0.005,
+                         precision=prec) as ctx:
+            ctx.set_w(wa, wb)
+            ctx.get_conc()
+            out[prec] = (ctx.pha, ctx.Q())
+    assert rel(out[1][0], out[0][0]) < 1e-5
+    assert abs(out[1][1][0] / out[0][1][0] - 1) < 1e-5
+
+
+def test_file_io_roundtrip(pkg, tmp_path):
+    g = GRIDS[1]
+    rng = np.random.default_rng(0)
+    with make_ctx(pkg, g, 0) as ctx:
+        wa, wb = rng.normal(0, 1, (2,) + ctx.shape)
+        ctx.set_w(wa, wb)
+        ctx.get_conc()
+        f = str(tmp_path / "pha_2.dat")
+        ctx.write_pha_dat(f, 1)
+        pha = ctx.pha
+        ctx.set_w(np.zeros(ctx.shape), np.zeros(ctx.shape))
+        ctx.read_phi_dat(f, 0)
+        np.testing.assert_allclose(ctx.wa[0], wa[1], rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(ctx.pha[0], pha[1], rtol=1e-5, atol=1e-6)
+        assert np.all(ctx.wa[1] == 0)
+
+
+def test_error_paths(pkg):
+    g = GRIDS[0]
+    with make_ctx(pkg, g, 0) as ctx:
+        with pytest.raises(pkg.ScftError) as e:
+            ctx.sov_dif_fft(pkg.Q_A, pkg.FIELD_WA, ctx.NsA + 1, 1)
+        assert e.value.status == pkg.ERR_INVALID_ARG
+        with pytest.raises(pkg.ScftError):
+            ctx.sov_dif_fft(pkg.Q_A, pkg.FIELD_WA, 1, 0)
+        with pytest.raises(pkg.ScftError) as e:
+            ctx.read_phi_dat("/nonexistent/phi_1.dat")
+        assert e.value.status == pkg.ERR_IO
+        # a NaN field is reported, not propagated silently
+        bad = np.zeros(ctx.shape)
+        bad[0, 0, 0, 0] = np.nan
+        ctx.set_w(bad, bad)
+        ctx.get_conc()
+        with pytest.raises(pkg.ScftError) as e:
+            ctx.free_energy()
+        assert e.value.status == pkg.ERR_NOT_FINITE
+        # the context stays usable afterwards
+        ctx.set_w(np.zeros(ctx.shape), np.zeros(ctx.shape))
+        ctx.get_conc()
+        assert abs(ctx.Q()[0] - 1) < 1e-12
