@@ -178,11 +178,13 @@ def run_ours(args):
         dist.init_process_group("nccl")
     dev = local if ws > 1 else 0
     prec = pkg.PREC_FP64 if args.precision == "fp64" else pkg.PREC_FP32
-    ctx = pkg.Context(nx=N, ny=N, nz=N, lx=L, ly=L, lz=L, hAB=CHIN, fA=FA, ds0=DS,
+    n, ds = args.grid, 1.0 / args.ns
+    headline = (n == N and args.ns == 200)
+    ctx = pkg.Context(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, hAB=CHIN, fA=FA, ds0=ds,
                       precision=prec, device=dev)
-    wa, wb = fl.gyroid(N, N, N, L, L, L, CHIN, seed=rank)
+    wa, wb = fl.gyroid(n, n, n, L, L, L, CHIN, seed=rank)
     ctx.set_w(wa, wb)
-    pt_steps = 2 * (ctx.NsA + ctx.dNsB) * N ** 3
+    pt_steps = 2 * (ctx.NsA + ctx.dNsB) * n ** 3
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -215,46 +217,55 @@ def run_ours(args):
     value = ws * pt_steps * args.steps / (t_max / 1e3) / 1e9
 
     # ---- end-to-end through the C ABI with pinned host buffers
-    hw_a = torch.from_numpy(wa.reshape(-1)).pin_memory()
-    hw_b = torch.from_numpy(wb.reshape(-1)).pin_memory()
-    ho_a = torch.empty(N ** 3, dtype=torch.float64).pin_memory()
-    ho_b = torch.empty(N ** 3, dtype=torch.float64).pin_memory()
-    import ctypes as C
-    dptr = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_double))
-    out5 = np.empty(5)
-    e2e_steps = max(1, min(args.steps, 5))
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        ctx._ck(ctx.lib.scft_set_field(ctx.h, pkg.FIELD_WA, dptr(hw_a)))
-        ctx._ck(ctx.lib.scft_set_field(ctx.h, pkg.FIELD_WB, dptr(hw_b)))
-        ctx._ck(ctx.lib.scft_iterate(ctx.h, 1, out5.ctypes.data_as(C.POINTER(C.c_double))))
-        ctx._ck(ctx.lib.scft_get_field(ctx.h, pkg.FIELD_PHA, dptr(ho_a)))
-        ctx._ck(ctx.lib.scft_get_field(ctx.h, pkg.FIELD_PHB, dptr(ho_b)))
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = ws * pt_steps * e2e_steps / e2e_s / 1e9
+    e2e = None
+    if not args.no_e2e:
+        hw_a = torch.from_numpy(wa.reshape(-1)).pin_memory()
+        hw_b = torch.from_numpy(wb.reshape(-1)).pin_memory()
+        ho_a = torch.empty(n ** 3, dtype=torch.float64).pin_memory()
+        ho_b = torch.empty(n ** 3, dtype=torch.float64).pin_memory()
+        import ctypes as C
+        dptr = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_double))
+        out5 = np.empty(5)
+        e2e_steps = max(1, min(args.steps, 5))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ctx._ck(ctx.lib.scft_set_field(ctx.h, pkg.FIELD_WA, dptr(hw_a)))
+            ctx._ck(ctx.lib.scft_set_field(ctx.h, pkg.FIELD_WB, dptr(hw_b)))
+            ctx._ck(ctx.lib.scft_iterate(ctx.h, 1, out5.ctypes.data_as(C.POINTER(C.c_double))))
+            ctx._ck(ctx.lib.scft_get_field(ctx.h, pkg.FIELD_PHA, dptr(ho_a)))
+            ctx._ck(ctx.lib.scft_get_field(ctx.h, pkg.FIELD_PHB, dptr(ho_b)))
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([e2e_s], device=f"cuda:{dev}", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": ws * pt_steps * e2e_steps / e2e_s / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": 2 * 8 * n ** 3, "d2h_bytes_per_step": 2 * 8 * n ** 3 + 5 * 8,
+               "steps": e2e_steps,
+               "path": "scft_set_field x2 (pinned host) + scft_iterate(1) + scft_get_field x2"}
 
     if rank == 0:
         peak, peak_kind = load_peaks()
         bpp = BYTES_PER_PT_STEP[args.precision]
         march_rate = march_pts / (march_ms / 1e3)          # pt-steps/s inside marches
         achieved = march_rate * bpp / 1e9                  # GB/s, algorithmic bytes
+        workload = WORKLOAD if headline else (
+            f"{n}^3 gyroid (f=0.36, chiN=18, box 3.8), Ns={args.ns}: a reduced case for "
+            f"profiling, not the headline")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if args.precision == "fp32" else "f64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "grid": [N, N, N], "Ns": 200, "batch": 1,
+            "config": {"workload": workload, "grid": [n, n, n], "Ns": args.ns, "batch": 1,
                        "propagation": args.precision,
                        "reductions": "fp64 (Q, F, mixing); phi contour sum compensated",
-                       "l2": "inputs larger than L2: each step streams 3.2 GB of propagator "
-                             "slices (fp32) through HBM",
+                       "l2": "inputs larger than L2: each step streams %.1f GB of propagator "
+                             "slices through HBM" % (4 * (ctx.NsA + ctx.dNsB + 2) * n ** 3 *
+                                                     (4 if args.precision == "fp32" else 8) / 1e9),
                        "parallelism": f"replicas x{ws} (no exchange step)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
@@ -264,8 +275,7 @@ def run_ours(args):
                          "march_ms_avg": march_ms / max(n_marches, 1),
                          "marches_timed": n_marches},
             "cpu_baseline": cpu_baseline() if not args.no_cpu else None,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * N ** 3,
-                    "d2h_bytes_per_step": 2 * 8 * N ** 3 + 5 * 8, "steps": e2e_steps},
+            "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk,
             "wall_s_timed": wall,
@@ -285,6 +295,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--grid", type=int, default=N, help="grid edge (profiling cases only)")
+    ap.add_argument("--ns", type=int, default=200, help="contour steps 1/ds (profiling only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

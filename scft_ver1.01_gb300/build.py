@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 
-SOURCES = ["capi.cu", "io.cpp", "k_line.cu", "k_fields.cu"]
+SOURCES = ["capi.cu", "io.cpp", "k_line.cu", "k_fields.cu", "k_fast.cu"]
 
 
 def nvcc() -> str:

@@ -67,19 +67,31 @@ bool axis_ok(int n, bool allow_one) {
 }
 
 template <typename R>
-int march_t(scft_ctx *ctx, int qi, const double *w, int ns, int sign) {
+cudaError_t launch_pass(const AxisPlan &ap, const R *in, long long ibs, R *out, long long obs,
+                        const R *pre, const R *post, long long wbs, int B, cudaStream_t st) {
+  if constexpr (sizeof(R) == 4) {
+    if (ap.use_fast) return scft::launch_fast_line(ap, in, ibs, out, obs, pre, post, wbs, B, st);
+  }
+  return scft::launch_line_filter<R>(ap, in, ibs, out, obs, pre, post, wbs, B, st);
+}
+
+// One propagator march (sovDifFft, cuda_scft.cu:435-563) of ns steps with the
+// Boltzmann factor W, on stream st.  init: the boundary slice (qInt), or null
+// for qInt = 1 (qInt_init, cuda_aid.cu:197-208).
+template <typename R>
+int march_t(scft_ctx *ctx, int qi, const R *W, const R *init, long long init_bs, int ns,
+            int sign, cudaStream_t st, int chain) {
   const long long M = ctx->M;
   const int B = ctx->batch;
   R *q = static_cast<R *>(ctx->q[qi]);
   const long long qbs = (long long)(ctx->q_ns[qi] + 1) * M;
-  R *W = static_cast<R *>(ctx->W);
-  R *qint = static_cast<R *>(ctx->qint);
-  R *tmp[2] = {static_cast<R *>(ctx->tmp[0]), static_cast<R *>(ctx->tmp[1])};
-  // initilize_wdz (cuda_scft.cu:450)
-  CKL(scft::launch_boltzmann<R>(w, W, M * B, ctx->p.ds0 / 2, ctx->st));
+  R *tmp[2] = {static_cast<R *>(ctx->tmp[2 * chain]), static_cast<R *>(ctx->tmp[2 * chain + 1])};
   // initilize_q / initilize_q_inverse (cuda_scft.cu:463,513)
   const int s0 = sign > 0 ? 0 : ns;
-  CKL(scft::launch_copy_slice<R>(q + (long long)s0 * M, qbs, qint, M, M, B, ctx->st));
+  if (init)
+    CKL(scft::launch_copy_slice<R>(q + (long long)s0 * M, qbs, init, init_bs, M, B, st));
+  else
+    CKL(scft::launch_fill<R>(q + (long long)s0 * M, M, R(1), qbs, B, st));
   const int np = (int)ctx->passes.size();
   for (int it = 1; it <= ns; ++it) {
     const int dst = sign > 0 ? it : ns - it;
@@ -89,11 +101,50 @@ int march_t(scft_ctx *ctx, int qi, const double *w, int ns, int sign) {
       const long long ibs = pi == 0 ? qbs : M;
       R *out = pi == np - 1 ? q + (long long)dst * M : tmp[pi & 1];
       const long long obs = pi == np - 1 ? qbs : M;
-      CKL(scft::launch_line_filter<R>(ctx->passes[pi], in, ibs, out, obs, pi == 0 ? W : nullptr,
-                                      pi == np - 1 ? W : nullptr, M, B, ctx->st));
+      CKL(launch_pass<R>(ctx->passes[pi], in, ibs, out, obs, pi == 0 ? W : nullptr,
+                         pi == np - 1 ? W : nullptr, M, B, st));
     }
   }
   return SCFT_OK;
+}
+
+// initilize_wdz (cuda_scft.cu:450) for field f into W[f].
+int boltzmann(scft_ctx *ctx, int f, cudaStream_t st) {
+  const double *w = f == SCFT_FIELD_WA ? ctx->wa : ctx->wb;
+  if (ctx->rbytes == 4)
+    CKL(scft::launch_boltzmann<float>(w, static_cast<float *>(ctx->W[f]), ctx->M * ctx->batch,
+                                      ctx->p.ds0 / 2, st));
+  else
+    CKL(scft::launch_boltzmann<double>(w, static_cast<double *>(ctx->W[f]), ctx->M * ctx->batch,
+                                       ctx->p.ds0 / 2, st));
+  return SCFT_OK;
+}
+
+// march with W[w_field]; init = slice s of propagator iq (iq < 0: ones;
+// iq == 4: the qInt buffer).
+int march_dispatch(scft_ctx *ctx, int qi, int w_field, int iq, int is, int ns, int sign,
+                   cudaStream_t st, int chain) {
+  const long long M = ctx->M;
+  if (ctx->rbytes == 4) {
+    const float *init = nullptr;
+    long long ibs = M;
+    if (iq == 4) init = static_cast<const float *>(ctx->qint);
+    else if (iq >= 0) {
+      init = static_cast<const float *>(ctx->q[iq]) + (long long)is * M;
+      ibs = (long long)(ctx->q_ns[iq] + 1) * M;
+    }
+    return march_t<float>(ctx, qi, static_cast<const float *>(ctx->W[w_field]), init, ibs, ns,
+                          sign, st, chain);
+  }
+  const double *init = nullptr;
+  long long ibs = M;
+  if (iq == 4) init = static_cast<const double *>(ctx->qint);
+  else if (iq >= 0) {
+    init = static_cast<const double *>(ctx->q[iq]) + (long long)is * M;
+    ibs = (long long)(ctx->q_ns[iq] + 1) * M;
+  }
+  return march_t<double>(ctx, qi, static_cast<const double *>(ctx->W[w_field]), init, ibs, ns,
+                         sign, st, chain);
 }
 
 int prof_reserve(scft_ctx *ctx, size_t n_events) {
@@ -105,22 +156,28 @@ int prof_reserve(scft_ctx *ctx, size_t n_events) {
   return SCFT_OK;
 }
 
-int march(scft_ctx *ctx, int qi, int w_field, int ns, int sign) {
-  const double *w = w_field == SCFT_FIELD_WA ? ctx->wa : ctx->wb;
-  int rc;
-  if (ctx->profiling) {
-    if ((rc = prof_reserve(ctx, ctx->prof_used + 2))) return rc;
-    CK(cudaEventRecord(ctx->prof_events[ctx->prof_used], ctx->st));
-  }
-  rc = ctx->rbytes == 4 ? march_t<float>(ctx, qi, w, ns, sign)
-                        : march_t<double>(ctx, qi, w, ns, sign);
+int prof_begin(scft_ctx *ctx) {
+  if (!ctx->profiling) return SCFT_OK;
+  int rc = prof_reserve(ctx, ctx->prof_used + 2);
   if (rc) return rc;
-  if (ctx->profiling) {
-    CK(cudaEventRecord(ctx->prof_events[ctx->prof_used + 1], ctx->st));
-    ctx->prof_used += 2;
-    ctx->prof_point_steps += (double)ns * ctx->M * ctx->batch;
-  }
+  CK(cudaEventRecord(ctx->prof_events[ctx->prof_used], ctx->st));
   return SCFT_OK;
+}
+int prof_end(scft_ctx *ctx, double point_steps) {
+  if (!ctx->profiling) return SCFT_OK;
+  CK(cudaEventRecord(ctx->prof_events[ctx->prof_used + 1], ctx->st));
+  ctx->prof_used += 2;
+  ctx->prof_point_steps += point_steps;
+  return SCFT_OK;
+}
+
+// The public single march (scft_sov_dif_fft): W from the field, init = qInt.
+int march(scft_ctx *ctx, int qi, int w_field, int ns, int sign) {
+  int rc;
+  if ((rc = boltzmann(ctx, w_field, ctx->st))) return rc;
+  if ((rc = prof_begin(ctx))) return rc;
+  if ((rc = march_dispatch(ctx, qi, w_field, 4, 0, ns, sign, ctx->st, 0))) return rc;
+  return prof_end(ctx, (double)ns * ctx->M * ctx->batch);
 }
 
 int average(scft_ctx *ctx, double *data) {
@@ -173,16 +230,32 @@ int q_and_phi(scft_ctx *ctx) {
   return SCFT_OK;
 }
 
+// getConc (cuda_scft.cu:61-138).  The four marches form two independent
+// chains -- qA (from 1) then qB (from qA[NsA]), and q+B (from 1) then q+A
+// (from q+B[0]) -- which run concurrently on two streams; each march gets the
+// same inputs as in the reference's sequential order, so the results are
+// identical.
 int get_conc(scft_ctx *ctx) {
   int rc;
   if ((rc = average(ctx, ctx->wa))) return rc;                                 // :71
-  if ((rc = set_qint(ctx, -1, 0))) return rc;                                  // :77
-  if ((rc = march(ctx, SCFT_Q_A, SCFT_FIELD_WA, ctx->NsA, 1))) return rc;      // :83
-  if ((rc = march(ctx, SCFT_Q_CB, SCFT_FIELD_WB, ctx->dNsB, -1))) return rc;   // :86
-  if ((rc = set_qint(ctx, SCFT_Q_A, ctx->NsA))) return rc;                     // :93
-  if ((rc = march(ctx, SCFT_Q_B, SCFT_FIELD_WB, ctx->dNsB, 1))) return rc;     // :99
-  if ((rc = set_qint(ctx, SCFT_Q_CB, 0))) return rc;                           // :106
-  if ((rc = march(ctx, SCFT_Q_CA, SCFT_FIELD_WA, ctx->NsA, -1))) return rc;    // :112
+  if ((rc = boltzmann(ctx, SCFT_FIELD_WA, ctx->st))) return rc;                // :450
+  if ((rc = boltzmann(ctx, SCFT_FIELD_WB, ctx->st))) return rc;
+  if ((rc = prof_begin(ctx))) return rc;
+  CK(cudaEventRecord(ctx->ev_fork, ctx->st));
+  CK(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
+  // chain 1 (main stream): qa (:83), qb from qa[NsA] (:93, :99)
+  if ((rc = march_dispatch(ctx, SCFT_Q_A, SCFT_FIELD_WA, -1, 0, ctx->NsA, 1, ctx->st, 0))) return rc;
+  if ((rc = march_dispatch(ctx, SCFT_Q_B, SCFT_FIELD_WB, SCFT_Q_A, ctx->NsA, ctx->dNsB, 1,
+                           ctx->st, 0)))
+    return rc;
+  // chain 2 (second stream): qcb (:86), qca from qcb[0] (:106, :112)
+  if ((rc = march_dispatch(ctx, SCFT_Q_CB, SCFT_FIELD_WB, -1, 0, ctx->dNsB, -1, ctx->st2, 1)))
+    return rc;
+  if ((rc = march_dispatch(ctx, SCFT_Q_CA, SCFT_FIELD_WA, SCFT_Q_CB, 0, ctx->NsA, -1, ctx->st2, 1)))
+    return rc;
+  CK(cudaEventRecord(ctx->ev_join, ctx->st2));
+  CK(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
+  if ((rc = prof_end(ctx, 2.0 * (ctx->NsA + ctx->dNsB) * ctx->M * ctx->batch))) return rc;
   return ctx->rbytes == 4 ? q_and_phi<float>(ctx) : q_and_phi<double>(ctx);
 }
 
@@ -220,7 +293,12 @@ int iterate_once(scft_ctx *ctx) {
 void free_all(scft_ctx *ctx) {
   cudaFree(ctx->wa); cudaFree(ctx->wb); cudaFree(ctx->pha); cudaFree(ctx->phb);
   for (int i = 0; i < 4; ++i) cudaFree(ctx->q[i]);
-  cudaFree(ctx->qint); cudaFree(ctx->W); cudaFree(ctx->tmp[0]); cudaFree(ctx->tmp[1]);
+  cudaFree(ctx->qint);
+  for (int i = 0; i < 2; ++i) cudaFree(ctx->W[i]);
+  for (int i = 0; i < 4; ++i) cudaFree(ctx->tmp[i]);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->st2) cudaStreamDestroy(ctx->st2);
   cudaFree(ctx->partial); cudaFree(ctx->sum); cudaFree(ctx->Q); cudaFree(ctx->ffl);
   cudaFree(ctx->fe5); cudaFree(ctx->tables);
   for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
@@ -322,9 +400,12 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     delete ctx;
     return scft_fail(nullptr, st, msg);
   };
-  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
     return fail(SCFT_ERR_CUDA, "stream creation failed");
-  if (scft::line_filter_prepare() != cudaSuccess)
+  if (scft::line_filter_prepare() != cudaSuccess || scft::fast_line_prepare() != cudaSuccess)
     return fail(SCFT_ERR_CUDA, "kernel attribute set-up failed");
 
   auto alloc = [&](void **ptr, size_t bytes) {
@@ -334,8 +415,9 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   bool ok = alloc((void **)&ctx->wa, 8 * M * B) && alloc((void **)&ctx->wb, 8 * M * B) &&
             alloc((void **)&ctx->pha, 8 * M * B) && alloc((void **)&ctx->phb, 8 * M * B);
   for (int i = 0; ok && i < 4; ++i) ok = alloc(&ctx->q[i], rb * M * B * (ctx->q_ns[i] + 1));
-  ok = ok && alloc(&ctx->qint, rb * M * B) && alloc(&ctx->W, rb * M * B) &&
-       alloc(&ctx->tmp[0], rb * M * B) && alloc(&ctx->tmp[1], rb * M * B);
+  ok = ok && alloc(&ctx->qint, rb * M * B) && alloc(&ctx->W[0], rb * M * B) &&
+       alloc(&ctx->W[1], rb * M * B);
+  for (int i = 0; ok && i < 4; ++i) ok = alloc(&ctx->tmp[i], rb * M * B);
   ctx->nblk = scft::reduce_blocks(M);
   ok = ok && alloc((void **)&ctx->partial, 8 * B * 3 * ctx->nblk) &&
        alloc((void **)&ctx->sum, 8 * B) && alloc((void **)&ctx->Q, 8 * B) &&
@@ -382,6 +464,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     if (tl < 1) tl = 1;
     if (tl > n_pairs) tl = n_pairs;
     ap.tl = tl;
+    ap.use_fast = (rb == 4 && scft::fast_line_supported(ap)) ? 1 : 0;
     if (scft::line_filter_smem_bytes(ap, rb) > (size_t)scft::kLineSmemMax)
       return fail(SCFT_ERR_UNSUPPORTED, "line too long for shared memory");
     // twiddles exp(-2 pi i m / n) and gains exp(-ds0 k^2)/n

@@ -11,29 +11,29 @@ template <typename R> struct cplx;
 template <> struct cplx<float> { typedef float2 type; };
 template <> struct cplx<double> { typedef double2 type; };
 
-template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
   C r;
   r.x = a.x * b.x - a.y * b.y;
   r.y = a.x * b.y + a.y * b.x;
   return r;
 }
-template <typename C> __device__ __forceinline__ C cadd(C a, C b) {
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) {
   C r; r.x = a.x + b.x; r.y = a.y + b.y; return r;
 }
-template <typename C> __device__ __forceinline__ C csub(C a, C b) {
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) {
   C r; r.x = a.x - b.x; r.y = a.y - b.y; return r;
 }
 // multiply by -i
-template <typename C> __device__ __forceinline__ C cmul_mi(C a) {
+template <typename C> __host__ __device__ __forceinline__ C cmul_mi(C a) {
   C r; r.x = a.y; r.y = -a.x; return r;
 }
-template <typename C, typename R> __device__ __forceinline__ C cscale(C a, R s) {
+template <typename C, typename R> __host__ __device__ __forceinline__ C cscale(C a, R s) {
   C r; r.x = a.x * s; r.y = a.y * s; return r;
 }
-template <typename C> __device__ __forceinline__ C cconj(C a) {
+template <typename C> __host__ __device__ __forceinline__ C cconj(C a) {
   C r; r.x = a.x; r.y = -a.y; return r;
 }
-template <typename C, typename R> __device__ __forceinline__ C mkc(R x, R y) {
+template <typename C, typename R> __host__ __device__ __forceinline__ C mkc(R x, R y) {
   C r; r.x = x; r.y = y; return r;
 }
 

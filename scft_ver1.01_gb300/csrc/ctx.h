@@ -15,7 +15,9 @@ struct scft_ctx {
   long long M = 0;
   int batch = 0;
   int rbytes = 8;               // sizeof working real (4 or 8)
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;    // main stream (all public entry points)
+  cudaStream_t st2 = nullptr;   // second march chain inside getConc
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::string err;
   long long launches = 0;
 
@@ -25,8 +27,8 @@ struct scft_ctx {
   void *q[4] = {nullptr, nullptr, nullptr, nullptr};
   int q_ns[4] = {0, 0, 0, 0};
   void *qint = nullptr;         // [batch][M]
-  void *W = nullptr;            // Boltzmann factor [batch][M]
-  void *tmp[2] = {nullptr, nullptr};
+  void *W[2] = {nullptr, nullptr};   // Boltzmann factors of wa / wb [batch][M]
+  void *tmp[4] = {nullptr, nullptr, nullptr, nullptr};  // pass intermediates, 2 per chain
   // reductions
   int nblk = 1;
   double *partial = nullptr;    // [batch][3][nblk]

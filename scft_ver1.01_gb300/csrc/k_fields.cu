@@ -39,12 +39,17 @@ __device__ __forceinline__ double block_max(double v, double *sh) {
   return r;
 }
 
+// initilize_wdz (cuda_aid.cu:254): W = exp(-w*ds2).  The FP32 factor is
+// evaluated in FP32 (GB300's FP64 pipe is narrow; the result is rounded to
+// FP32 anyway).
 template <typename R>
 __global__ void k_boltzmann(const double *__restrict__ w, R *__restrict__ W, long long n,
                             double ds2) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    W[i] = (R)exp(-w[i] * ds2);   // initilize_wdz, cuda_aid.cu:254
+       i += (long long)gridDim.x * blockDim.x) {
+    if constexpr (sizeof(R) == 4) W[i] = expf(-(float)w[i] * (float)ds2);
+    else W[i] = exp(-w[i] * ds2);
+  }
 }
 
 template <typename R>

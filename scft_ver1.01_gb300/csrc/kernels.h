@@ -22,9 +22,18 @@ struct AxisPlan {
   int n_outer;           // outer groups per instance
   int n_fast;            // 1: consecutive threads walk n (contiguous lines)
   int tl;                // complex lines per CTA tile
+  int use_fast;          // FP32 register-resident kernel (k_fast.cu) handles this pass
   const void *twiddle;   // device: n complex, exp(-2*pi*i*m/n), working precision
   const void *gain;      // device: n reals, working precision
 };
+
+// Register-resident FP32 pass (k_fast.cu): n in {32, 64, 128, 256} and
+// n_real a multiple of 64.
+bool fast_line_supported(const AxisPlan &ap);
+cudaError_t fast_line_prepare();
+cudaError_t launch_fast_line(const AxisPlan &ap, const float *in, long long in_bstride,
+                             float *out, long long out_bstride, const float *pre,
+                             const float *post, long long w_bstride, int batch, cudaStream_t st);
 
 // Generic mixed-radix Stockham line filter (any n whose prime factors are
 // <= 61).  in/out may not alias.  pre multiplies the input, post the output
