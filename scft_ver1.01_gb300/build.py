@@ -22,7 +22,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 
-SOURCES = ["capi.cu", "io.cpp", "k_line.cu", "k_fields.cu", "k_fast.cu"]
+SOURCES = ["capi.cu", "io.cpp", "compat.cpp", "k_line.cu", "k_fields.cu", "k_fast.cu"]
+# Drop-in driver of the reference's struct API (init_scft -> fft_test ->
+# finalize_cufft), linked against the library: the reference's `scan` binary.
+DRIVER_SRC = "scft_main.cpp"
+DRIVER = os.path.join(HERE, "scft_gb300_driver")
 
 
 def nvcc() -> str:
@@ -72,6 +76,10 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         list(ex.map(run, cmds))
     if cmds or _stale(LIB, objs):
         run([cc] + ARCH + ["-shared", "-o", LIB] + objs)
+    dsrc = os.path.join(CSRC, DRIVER_SRC)
+    if _stale(DRIVER, [dsrc, LIB] + hdrs):
+        run([cc] + NVCC_FLAGS + ["-I" + os.path.join(INCLUDE, "compat"), dsrc, "-o", DRIVER,
+                                 "-L" + HERE, "-lscft_gb300", "-Xlinker", "-rpath=$ORIGIN"])
     return LIB
 
 

@@ -1,0 +1,68 @@
+"""The drop-in driver of the struct API run as the reference binary is run:
+a directory with ab.txt and phi_<i>.dat (init.cpp:81-94,
+init_cuda.cu:435-456), flags -step=N; it prints the progress lines of Free
+(cuda_scft.cu:221) and time=, and writes pha_<i>.dat (cuda_scft.cu:233-243)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DRIVER = os.path.join(ROOT, "scft_ver1.01_gb300", "scft_gb300_driver")
+
+
+def write_case(orc, d, p, wa, wb):
+    with open(os.path.join(d, "ab.txt"), "w") as f:
+        f.write("intag=1024\nxN=%g\nfa=%.3f\nlx=%.15g, ly=%.15g, lz=%.15g\n"
+                "Nx=%d, Ny=%d, Nz=%d\nds0=%g\nbatch=%d\n"
+                % (p.hAB, p.fA, p.lx, p.ly, p.lz, p.nx, p.ny, p.nz, p.ds0, p.batch))
+    for i in range(p.batch):
+        z = np.zeros(p.M)
+        orc.write_pha_dat(os.path.join(d, "phi_%d.dat" % (i + 1)), p, z, z, wa[i].ravel(),
+                          wb[i].ravel())
+
+
+@pytest.mark.parametrize("prec,rtol", [("fp64", 1e-7), ("fp32", 2e-5)])
+def test_driver_matches_oracle(pkg, orc, tmp_path, prec, rtol):
+    assert os.path.exists(DRIVER), "driver not built"
+    from scft_gb300 import fields
+    p = orc.Params(nx=16, ny=16, nz=8, lx=4.0, ly=4.0, lz=2.0, hAB=20.0, fA=0.5, ds0=0.01,
+                   batch=2)
+    wa, wb = fields.lamellar(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 20.0, seed=4, batch=2)
+    d = str(tmp_path)
+    write_case(orc, d, p, wa, wb)
+    r = subprocess.run([DRIVER, "-step=100", "-precision=" + prec], cwd=d, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = [l for l in r.stdout.splitlines() if l.startswith("GPU ")]
+    assert len(lines) == 20                      # every 10 iterations x 2 instances
+    assert any(l.startswith("time=") for l in r.stdout.splitlines())
+    # the oracle starts from the same %g-rounded fields the driver read
+    wa0 = np.stack([orc.read_phi_dat(os.path.join(d, "phi_%d.dat" % (i + 1)), p.M)[2]
+                    for i in range(2)]).reshape((2,) + p.shape)
+    wb0 = np.stack([orc.read_phi_dat(os.path.join(d, "phi_%d.dat" % (i + 1)), p.M)[3]
+                    for i in range(2)]).reshape((2,) + p.shape)
+    ref = orc.free_loop(wa0, wb0, p, 100)
+    for l, row in zip(lines, ref.log):
+        it, b, F, fab, fw, fs, inc = row
+        assert l.startswith("GPU 0 batch %d: %5d :" % (b, it))
+        vals = [float(v) for v in l.split(":")[2].split(",")]
+        np.testing.assert_allclose(vals[:4], [F, fab, fw, fs], rtol=rtol, atol=1e-9)
+    for i in range(2):
+        path = os.path.join(d, "pha_%d.dat" % (i + 1))
+        assert os.path.exists(path)
+        head = open(path).read().splitlines()[:2]
+        assert head[0] == "Nx=16, Ny=16, Nz=8"
+        pa, pb, a, b = orc.read_phi_dat(path, p.M)
+        np.testing.assert_allclose(pa, ref.pha[i].ravel(), rtol=1e-4, atol=1e-5)
+        np.testing.assert_allclose(a, ref.wa[i].ravel(), rtol=1e-4, atol=1e-5)
+
+
+def test_driver_missing_config(pkg, tmp_path):
+    r = subprocess.run([DRIVER, "-step=1"], cwd=str(tmp_path), capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode != 0
+    assert "ab.txt did not exist" in r.stdout
