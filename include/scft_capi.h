@@ -72,8 +72,12 @@ typedef struct scft_params {
   int anderson_history;     /* Anderson history length (e.g. 20) */
   double anderson_lambda;   /* Anderson step on the residual */
   int device;               /* CUDA device ordinal */
-  int reserved[8];          /* must be zero */
+  int flags;                /* SCFT_FLAG_* */
+  int reserved[7];          /* must be zero */
 } scft_params;
+
+/* flags */
+#define SCFT_FLAG_NO_GRAPH 1      /* issue the march phase as plain launches, not a CUDA graph */
 
 /* Fill *p with the reference defaults (32^3, box 4, xN 20, fa 0.5,
  * ds0 0.01, batch 1, FP64, simple mixing wopt 0.05 wcmp 0.10). */

@@ -37,7 +37,8 @@ struct Ref {
          *qint = nullptr, *wdz = nullptr, *qa = nullptr, *qca = nullptr, *qb = nullptr,
          *qcb = nullptr, *ql = nullptr, *ffl = nullptr, *in = nullptr, *sum = nullptr;
   cufftDoubleComplex *out = nullptr;
-  std::vector<double> hql;
+  std::vector<double> hql, hql_raw;
+  int q_mode = 1;
   std::string err = "no error";
 };
 
@@ -178,6 +179,22 @@ int get_conc() {
   CR(cudaDeviceSynchronize());
   std::vector<double> ql(g.batch), ffl(g.batch);
   CR(cudaMemcpy(ql.data(), g.ql, sizeof(double) * g.batch, cudaMemcpyDeviceToHost));
+  g.hql_raw = ql;
+  // cal_ql stores each thread's partial (cuda_aid.cu:145) and starts the
+  // shared-memory tree (:149-158) without a barrier in between, so warps can
+  // read other warps' slots before they are written.  q_mode 1 replaces its
+  // result by the FP64 sum of the same slice qB[.][dNsB] (what cal_ql is meant
+  // to return); q_mode 0 keeps the kernel's value.
+  if (g.q_mode == 1) {
+    const long long ns1 = g.dNsB + 1;
+    std::vector<double> all(g.M * g.batch * ns1);
+    CR(cudaMemcpy(all.data(), g.qb, sizeof(double) * all.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < g.batch; i++) {
+      double s = 0.0;
+      for (long long r = 0; r < g.M; ++r) s += all[(r * ns1 + g.dNsB) + i * g.M * ns1];
+      ql[i] = s;
+    }
+  }
   for (int i = 0; i < g.batch; i++) {
     ql[i] /= g.M;
     ffl[i] = g.ds0 / ql[i];
@@ -315,6 +332,31 @@ int ref_get_field(int which, double *dst) {
 // Q per instance (ql/M after getConc)
 int ref_get_Q(double *dst) {
   for (int i = 0; i < g.batch; ++i) dst[i] = g.hql[i];
+  return 0;
+}
+// The raw cal_ql kernel result (sum, not divided by M) of the last getConc.
+int ref_get_ql_raw(double *dst) {
+  for (int i = 0; i < g.batch && i < (int)g.hql_raw.size(); ++i) dst[i] = g.hql_raw[i];
+  return 0;
+}
+// 0: use cal_ql's value as the reference does; 1 (default): FP64 sum of the
+// same qB slice (see get_conc).
+int ref_set_q_mode(int mode) {
+  g.q_mode = mode;
+  return 0;
+}
+// Runs the reference's cal_ql kernel `n` times back to back on the current
+// qB and returns each raw result for instance 0 (race diagnostics).
+int ref_cal_ql_repeat(int n, double *dst) {
+  int threads = 512;
+  unsigned smem = threads * sizeof(double) * 2;
+  int M = (int)g.M;
+  void *a3[] = {&g.ql, &g.qb, &g.dNsB, &M};
+  for (int k = 0; k < n; ++k) {
+    if (launch(g.f_cal_ql, dim3(g.batch), dim3(threads), smem, a3)) return 1;
+    CR(cudaDeviceSynchronize());
+    CR(cudaMemcpy(&dst[k], g.ql, sizeof(double), cudaMemcpyDeviceToHost));
+  }
   return 0;
 }
 // slice s of propagator which (0 qa, 1 qcb, 2 qb, 3 qca) as [batch][M]; the

@@ -88,6 +88,21 @@ class RefSolver:
         self._ck(self.lib.ref_iterate(n, self._p(out) if with_energy else None))
         return out if with_energy else None
 
+    def set_q_mode(self, mode):
+        """1 (default): Q from the FP64 sum of the reference's own qB slice;
+        0: the value of the reference's cal_ql kernel (which races)."""
+        self.lib.ref_set_q_mode(C.c_int(mode))
+
+    def ql_raw(self):
+        out = np.empty(self.shape[0])
+        self.lib.ref_get_ql_raw(self._p(out))
+        return out
+
+    def cal_ql_repeat(self, n):
+        out = np.empty(n)
+        self._ck(self.lib.ref_cal_ql_repeat(C.c_int(n), self._p(out)))
+        return out
+
     def time_iterations(self, n):
         ms = C.c_double()
         self._ck(self.lib.ref_time_iterations(n, C.byref(ms)))

@@ -48,7 +48,7 @@ class ScftParams(C.Structure):
         ("batch", C.c_int), ("precision", C.c_int),
         ("wopt", C.c_double), ("wcmp", C.c_double),
         ("mixing", C.c_int), ("anderson_history", C.c_int), ("anderson_lambda", C.c_double),
-        ("device", C.c_int), ("reserved", C.c_int * 8),
+        ("device", C.c_int), ("flags", C.c_int), ("reserved", C.c_int * 7),
     ]
 
 

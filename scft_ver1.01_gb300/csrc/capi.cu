@@ -66,46 +66,119 @@ bool axis_ok(int n, bool allow_one) {
   return radix_plan(n, fac, &nf);
 }
 
+// One pass over a set of propagators: a single launch of the register
+// kernel, or one generic launch per set member.
 template <typename R>
-cudaError_t launch_pass(const AxisPlan &ap, const R *in, long long ibs, R *out, long long obs,
-                        const R *pre, const R *post, long long wbs, int B, cudaStream_t st) {
+int launch_set(scft_ctx *ctx, const AxisPlan &ap, const scft::PassSet<R> &ps, cudaStream_t st) {
   if constexpr (sizeof(R) == 4) {
-    if (ap.use_fast) return scft::launch_fast_line(ap, in, ibs, out, obs, pre, post, wbs, B, st);
+    if (ap.use_fast) {
+      CKL(scft::launch_fast_line(ap, ps, st));
+      return SCFT_OK;
+    }
   }
-  return scft::launch_line_filter<R>(ap, in, ibs, out, obs, pre, post, wbs, B, st);
+  for (int k = 0; k < ps.nset; ++k)
+    CKL(scft::launch_line_filter<R>(ap, ps.in[k], ps.in_bs[k], ps.out[k], ps.out_bs[k],
+                                    ps.pre[k], ps.post[k], ps.w_bs, ps.batch, st));
+  return SCFT_OK;
 }
 
-// One propagator march (sovDifFft, cuda_scft.cu:435-563) of ns steps with the
-// Boltzmann factor W, on stream st.  init: the boundary slice (qInt), or null
-// for qInt = 1 (qInt_init, cuda_aid.cu:197-208).
+// A march segment: propagator qi over ns steps in field wf, direction sign,
+// starting from slice is of propagator iq (iq < 0: qInt = 1, qInt_init,
+// cuda_aid.cu:197-208; iq == 4: the qInt buffer).
+struct Seg {
+  int qi, wf, iq, is, ns, sign;
+};
+
+// initilize_q / initilize_q_inverse (cuda_scft.cu:463,513) of a segment.
 template <typename R>
-int march_t(scft_ctx *ctx, int qi, const R *W, const R *init, long long init_bs, int ns,
-            int sign, cudaStream_t st, int chain) {
+int seg_boundary(scft_ctx *ctx, const Seg &s, cudaStream_t st) {
   const long long M = ctx->M;
   const int B = ctx->batch;
-  R *q = static_cast<R *>(ctx->q[qi]);
-  const long long qbs = (long long)(ctx->q_ns[qi] + 1) * M;
-  R *tmp[2] = {static_cast<R *>(ctx->tmp[2 * chain]), static_cast<R *>(ctx->tmp[2 * chain + 1])};
-  // initilize_q / initilize_q_inverse (cuda_scft.cu:463,513)
-  const int s0 = sign > 0 ? 0 : ns;
-  if (init)
-    CKL(scft::launch_copy_slice<R>(q + (long long)s0 * M, qbs, init, init_bs, M, B, st));
-  else
-    CKL(scft::launch_fill<R>(q + (long long)s0 * M, M, R(1), qbs, B, st));
+  R *q = static_cast<R *>(ctx->q[s.qi]);
+  const long long qbs = (long long)(ctx->q_ns[s.qi] + 1) * M;
+  R *dst = q + (long long)(s.sign > 0 ? 0 : s.ns) * M;
+  if (s.iq < 0) {
+    CKL(scft::launch_fill<R>(dst, M, R(1), qbs, B, st));
+  } else {
+    const R *src = s.iq == 4 ? static_cast<const R *>(ctx->qint)
+                             : static_cast<const R *>(ctx->q[s.iq]) + (long long)s.is * M;
+    const long long sbs = s.iq == 4 ? M : (long long)(ctx->q_ns[s.iq] + 1) * M;
+    CKL(scft::launch_copy_slice<R>(dst, qbs, src, sbs, M, B, st));
+  }
+  return SCFT_OK;
+}
+
+// Runs up to kMaxSet chains of march segments in lockstep: contour step t of
+// every chain is one set of pass launches (sovDifFft's per-step
+// initilize_in_go -> D2Z -> sufaceField_go -> Z2D -> in_to_g_go,
+// cuda_scft.cu:467-491, as one line-filter pass per axis).  Chains are
+// independent, so the interleaving does not change any result.
+template <typename R>
+int run_chains(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nchain,
+               cudaStream_t st) {
+  const long long M = ctx->M;
+  int total[scft::kMaxSet] = {0, 0};
+  int maxT = 0;
+  for (int c = 0; c < nchain; ++c) {
+    for (int k = 0; k < nseg[c]; ++k) total[c] += chains[c][k].ns;
+    if (total[c] > maxT) maxT = total[c];
+    int rc = seg_boundary<R>(ctx, chains[c][0], st);
+    if (rc) return rc;
+  }
   const int np = (int)ctx->passes.size();
-  for (int it = 1; it <= ns; ++it) {
-    const int dst = sign > 0 ? it : ns - it;
-    const int src = sign > 0 ? dst - 1 : dst + 1;
+  for (int t = 1; t <= maxT; ++t) {
+    scft::PassSet<R> ps[3];
+    int nact = 0;
+    R *q_dst[scft::kMaxSet];
+    const R *q_src[scft::kMaxSet], *W[scft::kMaxSet];
+    long long qbs[scft::kMaxSet];
+    int cidx[scft::kMaxSet];
+    for (int c = 0; c < nchain; ++c) {
+      if (t > total[c]) continue;
+      int k = 0, it = t;
+      while (it > chains[c][k].ns) it -= chains[c][k++].ns;
+      const Seg &s = chains[c][k];
+      if (it == 1 && k > 0) {
+        int rc = seg_boundary<R>(ctx, s, st);
+        if (rc) return rc;
+      }
+      const int dst = s.sign > 0 ? it : s.ns - it;
+      const int src = s.sign > 0 ? dst - 1 : dst + 1;
+      R *q = static_cast<R *>(ctx->q[s.qi]);
+      qbs[nact] = (long long)(ctx->q_ns[s.qi] + 1) * M;
+      q_dst[nact] = q + (long long)dst * M;
+      q_src[nact] = q + (long long)src * M;
+      W[nact] = static_cast<const R *>(ctx->W[s.wf]);
+      cidx[nact] = c;
+      ++nact;
+    }
     for (int pi = 0; pi < np; ++pi) {
-      const R *in = pi == 0 ? q + (long long)src * M : tmp[(pi - 1) & 1];
-      const long long ibs = pi == 0 ? qbs : M;
-      R *out = pi == np - 1 ? q + (long long)dst * M : tmp[pi & 1];
-      const long long obs = pi == np - 1 ? qbs : M;
-      CKL(launch_pass<R>(ctx->passes[pi], in, ibs, out, obs, pi == 0 ? W : nullptr,
-                         pi == np - 1 ? W : nullptr, M, B, st));
+      scft::PassSet<R> &p = ps[pi];
+      memset(&p, 0, sizeof(p));
+      p.nset = nact;
+      p.batch = ctx->batch;
+      p.w_bs = M;
+      for (int a = 0; a < nact; ++a) {
+        R *tmp0 = static_cast<R *>(ctx->tmp[2 * cidx[a]]);
+        R *tmp1 = static_cast<R *>(ctx->tmp[2 * cidx[a] + 1]);
+        p.in[a] = pi == 0 ? q_src[a] : ((pi - 1) & 1 ? tmp1 : tmp0);
+        p.in_bs[a] = pi == 0 ? qbs[a] : M;
+        p.out[a] = pi == np - 1 ? q_dst[a] : (pi & 1 ? tmp1 : tmp0);
+        p.out_bs[a] = pi == np - 1 ? qbs[a] : M;
+        p.pre[a] = pi == 0 ? W[a] : nullptr;
+        p.post[a] = pi == np - 1 ? W[a] : nullptr;
+      }
+      int rc = launch_set<R>(ctx, ctx->passes[pi], p, st);
+      if (rc) return rc;
     }
   }
   return SCFT_OK;
+}
+
+int run_chains_any(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nchain,
+                   cudaStream_t st) {
+  return ctx->rbytes == 4 ? run_chains<float>(ctx, chains, nseg, nchain, st)
+                          : run_chains<double>(ctx, chains, nseg, nchain, st);
 }
 
 // initilize_wdz (cuda_scft.cu:450) for field f into W[f].
@@ -120,31 +193,48 @@ int boltzmann(scft_ctx *ctx, int f, cudaStream_t st) {
   return SCFT_OK;
 }
 
-// march with W[w_field]; init = slice s of propagator iq (iq < 0: ones;
-// iq == 4: the qInt buffer).
-int march_dispatch(scft_ctx *ctx, int qi, int w_field, int iq, int is, int ns, int sign,
-                   cudaStream_t st, int chain) {
-  const long long M = ctx->M;
-  if (ctx->rbytes == 4) {
-    const float *init = nullptr;
-    long long ibs = M;
-    if (iq == 4) init = static_cast<const float *>(ctx->qint);
-    else if (iq >= 0) {
-      init = static_cast<const float *>(ctx->q[iq]) + (long long)is * M;
-      ibs = (long long)(ctx->q_ns[iq] + 1) * M;
+// The march phase of getConc (cuda_scft.cu:77-112) as two lockstep chains:
+// qA (from 1) then qB (from qA[NsA]); q+B (from 1) then q+A (from q+B[0]).
+// Each march gets exactly the inputs of the reference's sequential order.
+int march_phase(scft_ctx *ctx, cudaStream_t st) {
+  const Seg c0[2] = {{SCFT_Q_A, SCFT_FIELD_WA, -1, 0, ctx->NsA, 1},
+                     {SCFT_Q_B, SCFT_FIELD_WB, SCFT_Q_A, ctx->NsA, ctx->dNsB, 1}};
+  const Seg c1[2] = {{SCFT_Q_CB, SCFT_FIELD_WB, -1, 0, ctx->dNsB, -1},
+                     {SCFT_Q_CA, SCFT_FIELD_WA, SCFT_Q_CB, 0, ctx->NsA, -1}};
+  const Seg *chains[2] = {c0, c1};
+  const int nseg[2] = {2, 2};
+  return run_chains_any(ctx, chains, nseg, 2, st);
+}
+
+// The march phase through a CUDA graph captured on first use (the pointers
+// and step counts of a context never change), so one launch replays the
+// ~3*(NsA+dNsB) kernels of the phase.
+int march_phase_graph(scft_ctx *ctx) {
+  if (!ctx->use_graph) return march_phase(ctx, ctx->st);
+  if (!ctx->march_exec) {
+    const long long l0 = ctx->launches;
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    int rc = march_phase(ctx, ctx->st);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->st, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
     }
-    return march_t<float>(ctx, qi, static_cast<const float *>(ctx->W[w_field]), init, ibs, ns,
-                          sign, st, chain);
+    if (e != cudaSuccess)
+      return scft_fail(ctx, SCFT_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&ctx->march_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      ctx->march_exec = nullptr;
+      return scft_fail(ctx, SCFT_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    ctx->march_nodes = ctx->launches - l0;
+    ctx->launches = l0;
   }
-  const double *init = nullptr;
-  long long ibs = M;
-  if (iq == 4) init = static_cast<const double *>(ctx->qint);
-  else if (iq >= 0) {
-    init = static_cast<const double *>(ctx->q[iq]) + (long long)is * M;
-    ibs = (long long)(ctx->q_ns[iq] + 1) * M;
-  }
-  return march_t<double>(ctx, qi, static_cast<const double *>(ctx->W[w_field]), init, ibs, ns,
-                         sign, st, chain);
+  CK(cudaGraphLaunch(ctx->march_exec, ctx->st));
+  ctx->launches += ctx->march_nodes;
+  return SCFT_OK;
 }
 
 int prof_reserve(scft_ctx *ctx, size_t n_events) {
@@ -176,7 +266,10 @@ int march(scft_ctx *ctx, int qi, int w_field, int ns, int sign) {
   int rc;
   if ((rc = boltzmann(ctx, w_field, ctx->st))) return rc;
   if ((rc = prof_begin(ctx))) return rc;
-  if ((rc = march_dispatch(ctx, qi, w_field, 4, 0, ns, sign, ctx->st, 0))) return rc;
+  const Seg s[1] = {{qi, w_field, 4, 0, ns, sign}};
+  const Seg *chains[1] = {s};
+  const int nseg[1] = {1};
+  if ((rc = run_chains_any(ctx, chains, nseg, 1, ctx->st))) return rc;
   return prof_end(ctx, (double)ns * ctx->M * ctx->batch);
 }
 
@@ -230,31 +323,16 @@ int q_and_phi(scft_ctx *ctx) {
   return SCFT_OK;
 }
 
-// getConc (cuda_scft.cu:61-138).  The four marches form two independent
-// chains -- qA (from 1) then qB (from qA[NsA]), and q+B (from 1) then q+A
-// (from q+B[0]) -- which run concurrently on two streams; each march gets the
-// same inputs as in the reference's sequential order, so the results are
-// identical.
+// getConc (cuda_scft.cu:61-138): average_value(wa), the Boltzmann factors
+// (initilize_wdz, :450, once per field instead of once per march), the march
+// phase, then Q and the contour sums.
 int get_conc(scft_ctx *ctx) {
   int rc;
   if ((rc = average(ctx, ctx->wa))) return rc;                                 // :71
-  if ((rc = boltzmann(ctx, SCFT_FIELD_WA, ctx->st))) return rc;                // :450
+  if ((rc = boltzmann(ctx, SCFT_FIELD_WA, ctx->st))) return rc;
   if ((rc = boltzmann(ctx, SCFT_FIELD_WB, ctx->st))) return rc;
   if ((rc = prof_begin(ctx))) return rc;
-  CK(cudaEventRecord(ctx->ev_fork, ctx->st));
-  CK(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
-  // chain 1 (main stream): qa (:83), qb from qa[NsA] (:93, :99)
-  if ((rc = march_dispatch(ctx, SCFT_Q_A, SCFT_FIELD_WA, -1, 0, ctx->NsA, 1, ctx->st, 0))) return rc;
-  if ((rc = march_dispatch(ctx, SCFT_Q_B, SCFT_FIELD_WB, SCFT_Q_A, ctx->NsA, ctx->dNsB, 1,
-                           ctx->st, 0)))
-    return rc;
-  // chain 2 (second stream): qcb (:86), qca from qcb[0] (:106, :112)
-  if ((rc = march_dispatch(ctx, SCFT_Q_CB, SCFT_FIELD_WB, -1, 0, ctx->dNsB, -1, ctx->st2, 1)))
-    return rc;
-  if ((rc = march_dispatch(ctx, SCFT_Q_CA, SCFT_FIELD_WA, SCFT_Q_CB, 0, ctx->NsA, -1, ctx->st2, 1)))
-    return rc;
-  CK(cudaEventRecord(ctx->ev_join, ctx->st2));
-  CK(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
+  if ((rc = march_phase_graph(ctx))) return rc;                                // :77-112
   if ((rc = prof_end(ctx, 2.0 * (ctx->NsA + ctx->dNsB) * ctx->M * ctx->batch))) return rc;
   return ctx->rbytes == 4 ? q_and_phi<float>(ctx) : q_and_phi<double>(ctx);
 }
@@ -296,9 +374,8 @@ void free_all(scft_ctx *ctx) {
   cudaFree(ctx->qint);
   for (int i = 0; i < 2; ++i) cudaFree(ctx->W[i]);
   for (int i = 0; i < 4; ++i) cudaFree(ctx->tmp[i]);
-  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
-  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
-  if (ctx->st2) cudaStreamDestroy(ctx->st2);
+  if (ctx->march_exec) cudaGraphExecDestroy(ctx->march_exec);
+  ctx->march_exec = nullptr;
   cudaFree(ctx->partial); cudaFree(ctx->sum); cudaFree(ctx->Q); cudaFree(ctx->ffl);
   cudaFree(ctx->fe5); cudaFree(ctx->tables);
   for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
@@ -362,8 +439,9 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   if (!pin || !out) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "null argument");
   *out = nullptr;
   const scft_params &p = *pin;
-  for (int i = 0; i < 8; ++i)
+  for (int i = 0; i < 7; ++i)
     if (p.reserved[i]) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "reserved fields must be 0");
+  if (p.flags & ~SCFT_FLAG_NO_GRAPH) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad flags");
   if (!(p.lx > 0 && p.ly > 0 && p.lz > 0 && p.ds0 > 0 && p.fA >= 0 && p.fA <= 1 && p.batch >= 1))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
   if (p.precision != SCFT_PREC_FP64 && p.precision != SCFT_PREC_FP32)
@@ -400,10 +478,8 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     delete ctx;
     return scft_fail(nullptr, st, msg);
   };
-  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
+  ctx->use_graph = (p.flags & SCFT_FLAG_NO_GRAPH) == 0;
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
     return fail(SCFT_ERR_CUDA, "stream creation failed");
   if (scft::line_filter_prepare() != cudaSuccess || scft::fast_line_prepare() != cudaSuccess)
     return fail(SCFT_ERR_CUDA, "kernel attribute set-up failed");

@@ -15,9 +15,10 @@ struct scft_ctx {
   long long M = 0;
   int batch = 0;
   int rbytes = 8;               // sizeof working real (4 or 8)
-  cudaStream_t st = nullptr;    // main stream (all public entry points)
-  cudaStream_t st2 = nullptr;   // second march chain inside getConc
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t st = nullptr;    // the context's stream (every launch)
+  bool use_graph = true;        // march phase replayed as a CUDA graph
+  cudaGraphExec_t march_exec = nullptr;
+  long long march_nodes = 0;    // kernel launches inside the graph
   std::string err;
   long long launches = 0;
 

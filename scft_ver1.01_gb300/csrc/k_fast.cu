@@ -24,18 +24,22 @@ namespace scft {
 namespace {
 
 template <int N, int P, bool XP>
-__global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, const float *__restrict__ in,
-                                                      long long in_bs, float *__restrict__ out,
-                                                      long long out_bs,
-                                                      const float *__restrict__ pre,
-                                                      const float *__restrict__ post,
-                                                      long long w_bs) {
+__global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float> ps) {
   constexpr int R1 = N / P;
   constexpr int NT = P * 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *ex = reinterpret_cast<float2 *>(smem_raw);
   const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
-  const long long b = blockIdx.z;
+  // blockIdx.z = set * batch + instance
+  const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
+  const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
+  const float *__restrict__ in = set ? ps.in[1] : ps.in[0];
+  float *__restrict__ out = set ? ps.out[1] : ps.out[0];
+  const float *__restrict__ pre = set ? ps.pre[1] : ps.pre[0];
+  const float *__restrict__ post = set ? ps.post[1] : ps.post[0];
+  const long long in_bs = set ? ps.in_bs[1] : ps.in_bs[0];
+  const long long out_bs = set ? ps.out_bs[1] : ps.out_bs[0];
+  const long long w_bs = ps.w_bs;
   const float2 *__restrict__ tw = reinterpret_cast<const float2 *>(ap.twiddle);
   const float *__restrict__ gain = reinterpret_cast<const float *>(ap.gain);
   float2 v[R1];
@@ -163,12 +167,9 @@ template <int N, int P, bool XP> size_t fast_smem() {
 }
 
 template <int N, int P, bool XP>
-cudaError_t launch_one(const AxisPlan &ap, const float *in, long long ibs, float *out,
-                       long long obs, const float *pre, const float *post, long long wbs,
-                       int batch, cudaStream_t st) {
-  dim3 grid(ap.n_real / 64, XP ? 1 : ap.n_outer, batch);
-  k_fast_line<N, P, XP><<<grid, P * 32, fast_smem<N, P, XP>(), st>>>(ap, in, ibs, out, obs, pre,
-                                                                      post, wbs);
+cudaError_t launch_one(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
+  dim3 grid(ap.n_real / 64, XP ? 1 : ap.n_outer, ps.nset * ps.batch);
+  k_fast_line<N, P, XP><<<grid, P * 32, fast_smem<N, P, XP>(), st>>>(ap, ps);
   return cudaGetLastError();
 }
 
@@ -197,21 +198,16 @@ cudaError_t fast_line_prepare() {
   return e;
 }
 
-cudaError_t launch_fast_line(const AxisPlan &ap, const float *in, long long ibs, float *out,
-                             long long obs, const float *pre, const float *post, long long wbs,
-                             int batch, cudaStream_t st) {
+cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
+  if (ps.nset < 1 || ps.nset > kMaxSet) return cudaErrorInvalidValue;
   const bool xp = ap.n_fast != 0;
   switch (ap.n) {
-    case 32: return xp ? launch_one<32, 4, true>(ap, in, ibs, out, obs, pre, post, wbs, batch, st)
-                       : launch_one<32, 4, false>(ap, in, ibs, out, obs, pre, post, wbs, batch, st);
-    case 64: return xp ? launch_one<64, 8, true>(ap, in, ibs, out, obs, pre, post, wbs, batch, st)
-                       : launch_one<64, 8, false>(ap, in, ibs, out, obs, pre, post, wbs, batch, st);
+    case 32: return xp ? launch_one<32, 4, true>(ap, ps, st) : launch_one<32, 4, false>(ap, ps, st);
+    case 64: return xp ? launch_one<64, 8, true>(ap, ps, st) : launch_one<64, 8, false>(ap, ps, st);
     case 128:
-      return xp ? launch_one<128, 8, true>(ap, in, ibs, out, obs, pre, post, wbs, batch, st)
-                : launch_one<128, 8, false>(ap, in, ibs, out, obs, pre, post, wbs, batch, st);
+      return xp ? launch_one<128, 8, true>(ap, ps, st) : launch_one<128, 8, false>(ap, ps, st);
     case 256:
-      return xp ? launch_one<256, 16, true>(ap, in, ibs, out, obs, pre, post, wbs, batch, st)
-                : launch_one<256, 16, false>(ap, in, ibs, out, obs, pre, post, wbs, batch, st);
+      return xp ? launch_one<256, 16, true>(ap, ps, st) : launch_one<256, 16, false>(ap, ps, st);
     default: return cudaErrorInvalidValue;
   }
 }

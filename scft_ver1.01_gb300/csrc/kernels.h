@@ -27,13 +27,26 @@ struct AxisPlan {
   const void *gain;      // device: n reals, working precision
 };
 
+// One pass over up to kMaxSet independent propagators at once (the lockstep
+// march chains): set k reads in[k] (+ b*in_bs), multiplies by pre[k], filters,
+// multiplies by post[k] and writes out[k] (+ b*out_bs), for every instance b.
+constexpr int kMaxSet = 2;
+template <typename R> struct PassSet {
+  const R *in[kMaxSet];
+  R *out[kMaxSet];
+  const R *pre[kMaxSet];
+  const R *post[kMaxSet];
+  long long in_bs[kMaxSet], out_bs[kMaxSet];
+  long long w_bs;
+  int nset;
+  int batch;
+};
+
 // Register-resident FP32 pass (k_fast.cu): n in {32, 64, 128, 256} and
 // n_real a multiple of 64.
 bool fast_line_supported(const AxisPlan &ap);
 cudaError_t fast_line_prepare();
-cudaError_t launch_fast_line(const AxisPlan &ap, const float *in, long long in_bstride,
-                             float *out, long long out_bstride, const float *pre,
-                             const float *post, long long w_bstride, int batch, cudaStream_t st);
+cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
 
 // Generic mixed-radix Stockham line filter (any n whose prime factors are
 // <= 61).  in/out may not alias.  pre multiplies the input, post the output

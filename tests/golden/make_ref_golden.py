@@ -7,6 +7,12 @@ For each case the seeded input fields and the reference outputs are written
 to tests/golden/ref_<case>.npz (or --out DIR).  tests/test_ref_golden.py then
 checks the oracle against them on the CPU.
 
+Q: the reference's cal_ql kernel (cuda_aid.cu:119-168) writes each thread's
+partial sum to shared memory and starts the tree reduction without a barrier,
+so on GB300 it returns a corrupted sum.  The harness therefore takes Q from the
+FP64 sum of the reference's own qB[.][dNsB] slice (q_mode 1) and records the
+kernel's raw value beside it (calql_raw, calql_repeat).
+
     python tests/golden/make_ref_golden.py [--out DIR] [--time]
 
 --time also prints the reference's own GPU time per SCF iteration at the
@@ -64,7 +70,10 @@ def run_case(case, outdir):
                wa_in=wa, wb_in=wb, conc_wa=r.get_field(0), conc_pha=r.get_field(2),
                conc_phb=r.get_field(3), conc_Q=r.Q(),
                qa_end=r.get_q(0, r.NsA), qcb_0=r.get_q(1, 0), qb_end=r.get_q(2, r.dNsB),
-               qca_0=r.get_q(3, 0), qca_mid=r.get_q(3, r.NsA // 2))
+               qca_0=r.get_q(3, 0), qca_mid=r.get_q(3, r.NsA // 2),
+               # the reference's cal_ql kernel value of that getConc, and five
+               # back-to-back re-runs of it on the same slice (its shared-memory race)
+               calql_raw=r.ql_raw(), calql_repeat=r.cal_ql_repeat(5))
     r.set_w(wa, wb)
     fe = r.iterate(iters)
     out.update(iters=iters, loop_wa=r.get_field(0), loop_wb=r.get_field(1),
@@ -93,6 +102,7 @@ def time_reference():
     n, L = 128, 3.8
     wa, wb = fields_for("gyroid", (n, n, n), (L, L, L), 18.0, 0, 1)
     r = RefSolver(n, n, n, L, L, L, 18.0, 0.36, 0.005, 1)
+    r.set_q_mode(0)        # time the reference exactly as it runs (cal_ql kernel)
     r.set_w(wa, wb)
     r.iterate(1, with_energy=False)          # warm-up (plans, modules)
     ms = r.time_iterations(2) / 2
