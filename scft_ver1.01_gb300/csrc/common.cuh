@@ -37,6 +37,31 @@ template <typename C, typename R> __host__ __device__ __forceinline__ C mkc(R x,
   C r; r.x = x; r.y = y; return r;
 }
 
+// Programmatic dependent launch.  A kernel launched with launch_pdl may start
+// while its predecessor in the stream is still running; it must call
+// pdl_wait() before touching anything the predecessor writes, and releases
+// its own dependents with pdl_release().
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // Warp-level sum of a double.
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

@@ -40,6 +40,9 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float
   const long long in_bs = set ? ps.in_bs[1] : ps.in_bs[0];
   const long long out_bs = set ? ps.out_bs[1] : ps.out_bs[0];
   const long long w_bs = ps.w_bs;
+  // the input slice is the previous pass's output
+  pdl_wait();
+  pdl_release();
   const float2 *__restrict__ tw = reinterpret_cast<const float2 *>(ap.twiddle);
   const float *__restrict__ gain = reinterpret_cast<const float *>(ap.gain);
   float2 v[R1];
@@ -169,8 +172,7 @@ template <int N, int P, bool XP> size_t fast_smem() {
 template <int N, int P, bool XP>
 cudaError_t launch_one(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
   dim3 grid(ap.n_real / 64, XP ? 1 : ap.n_outer, ps.nset * ps.batch);
-  k_fast_line<N, P, XP><<<grid, P * 32, fast_smem<N, P, XP>(), st>>>(ap, ps);
-  return cudaGetLastError();
+  return launch_pdl(k_fast_line<N, P, XP>, grid, dim3(P * 32), fast_smem<N, P, XP>(), st, ap, ps);
 }
 
 template <int N, int P, bool XP> cudaError_t prep_one() {

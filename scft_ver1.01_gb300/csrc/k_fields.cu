@@ -95,10 +95,12 @@ __global__ void k_finalize_sum(const double *__restrict__ partial, int nblk, dou
 __global__ void k_minus_average(double *__restrict__ data, const double *__restrict__ sum,
                                 long long M) {
   double *d = data + blockIdx.y * M;
-  const double s = sum[blockIdx.y];
+  // minus_average (cuda_aid.cu:377) divides per element; the quotient is the
+  // same for every element, so it is formed once (bit-identical result).
+  const double mean = sum[blockIdx.y] / (double)M;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
        i += (long long)gridDim.x * blockDim.x)
-    d[i] = d[i] - s / (double)M;   // minus_average, cuda_aid.cu:377
+    d[i] = d[i] - mean;
 }
 
 __global__ void k_q_ffl(const double *__restrict__ sum, long long M, double ds0, int batch,

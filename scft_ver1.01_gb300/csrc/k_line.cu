@@ -178,6 +178,8 @@ __global__ void __launch_bounds__(256) k_line_filter(AxisPlan ap, const R *__res
   R *rb0 = reinterpret_cast<R *>(buf0);
   const C *tw = reinterpret_cast<const C *>(ap.twiddle);
   const R *gain = reinterpret_cast<const R *>(ap.gain);
+  pdl_wait();      // the input slice is the previous pass's output
+  pdl_release();
 
   const long long base = (long long)outer * ap.s_outer;
   const R *inb = in + (long long)b * in_bs + base;
@@ -254,9 +256,8 @@ cudaError_t launch_line_filter(const AxisPlan &ap, const R *in, long long in_bst
   const int n_pairs = (ap.n_real + 1) >> 1;
   dim3 grid((n_pairs + ap.tl - 1) / ap.tl, ap.n_outer, batch);
   const size_t smem = line_filter_smem_bytes(ap, sizeof(R));
-  k_line_filter<R><<<grid, 256, smem, st>>>(ap, in, in_bstride, out, out_bstride, pre, post,
-                                            w_bstride);
-  return cudaGetLastError();
+  return launch_pdl(k_line_filter<R>, grid, dim3(256), smem, st, ap, in, in_bstride, out,
+                    out_bstride, pre, post, w_bstride);
 }
 
 template cudaError_t launch_line_filter<float>(const AxisPlan &, const float *, long long, float *,
