@@ -176,6 +176,27 @@ int scft_profile_enable(scft_ctx *ctx, int enable);
 int scft_profile_read(scft_ctx *ctx, double *march_ms, long long *n_marches,
                       double *point_steps);
 
+/* ---- split step without device allocation ----
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * where they advance a propagator: a framework that owns all device memory
+ * through its own pool, code running while a stream is captured into a CUDA
+ * graph, or loops that cannot afford cudaMalloc's implicit synchronisation.
+ * One FP32 split step q_out = W . IFFT[G . FFT[W . q_in]] / M (one contour
+ * step of sovDifFft, cuda_scft.cu:467-491) for `batch` instances laid out
+ * [batch][Nz][Ny][Nx]; q_in, W and q_out are caller-owned device buffers of
+ * batch*Nx*Ny*Nz floats (W: the Boltzmann factor exp(-w*ds0/2)), enqueued on
+ * `stream` (a cudaStream_t; NULL = default stream).  Scratch lives in a static
+ * device array of this library: batch*Nx*Ny*Nz is limited to 2^21 points
+ * (larger requests return SCFT_ERR_INVALID_ARG), every GPU that loads the
+ * library holds the array (~16 MB) until exit, and calls that overlap on the
+ * GPU race on it.  The first call on a device looks up the array's address;
+ * make it before any stream capture.  Never calls cudaMalloc/cudaFree. */
+int scft_split_step_noalloc(int nx, int ny, int nz, double lx, double ly, double lz, double ds0,
+                            int batch, const float *q_in, const float *W, float *q_out,
+                            void *stream);
+/* Message of the last failed scft_split_step_noalloc call. */
+const char *scft_noalloc_last_error(void);
+
 /* ---- file formats (drop-in I/O) ---- */
 
 /* Parse an ab.txt file (init.cpp:81-94) into *p (other fields default). */

@@ -36,6 +36,7 @@ EXPORTS = [
     "scft_get_Q", "scft_phi_w", "scft_free_energy", "scft_iterate", "scft_free",
     "scft_synchronize", "scft_launch_count", "scft_read_ab_txt", "scft_read_phi_dat",
     "scft_write_pha_dat", "scft_time_iterations", "scft_profile_enable", "scft_profile_read",
+    "scft_split_step_noalloc", "scft_noalloc_last_error",
 ]
 
 
@@ -100,6 +101,9 @@ def load_library(path: str | None = None):
         "scft_time_iterations": (C.c_int, [vp, C.c_int, dp]),
         "scft_profile_enable": (C.c_int, [vp, C.c_int]),
         "scft_profile_read": (C.c_int, [vp, dp, C.POINTER(C.c_longlong), dp]),
+        "scft_split_step_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                              C.c_double, C.c_double, C.c_int, vp, vp, vp, vp]),
+        "scft_noalloc_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
