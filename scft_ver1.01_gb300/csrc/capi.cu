@@ -158,6 +158,7 @@ int run_chains(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nch
       p.nset = nact;
       p.batch = ctx->batch;
       p.w_bs = M;
+      p.err = ctx->use_pipe ? ctx->dev_err : nullptr;
       for (int a = 0; a < nact; ++a) {
         R *tmp0 = static_cast<R *>(ctx->tmp[2 * cidx[a]]);
         R *tmp1 = static_cast<R *>(ctx->tmp[2 * cidx[a] + 1]);
@@ -351,10 +352,25 @@ int free_energy_dev(scft_ctx *ctx) {
   return SCFT_OK;
 }
 
+// Synchronise the stream and check the device error word that the pipelined
+// kernels set when a bounded wait gives up.
+int sync_check(scft_ctx *ctx) {
+  CK(cudaStreamSynchronize(ctx->st));
+  unsigned w = 0;
+  CK(cudaMemcpy(&w, ctx->dev_err, sizeof(w), cudaMemcpyDeviceToHost));
+  if (w) {
+    cudaMemset(ctx->dev_err, 0, sizeof(unsigned));
+    return scft_fail(ctx, SCFT_ERR_CUDA,
+                     "a pipelined kernel timed out waiting for its bulk copies (error word " +
+                         std::to_string(w) + "); results of that launch are invalid");
+  }
+  return SCFT_OK;
+}
+
 int read_fe(scft_ctx *ctx, double *out5) {
   CK(cudaMemcpyAsync(out5, ctx->fe5, sizeof(double) * 5 * ctx->batch, cudaMemcpyDeviceToHost,
                      ctx->st));
-  CK(cudaStreamSynchronize(ctx->st));
+  if (int rc = sync_check(ctx)) return rc;
   for (int i = 0; i < 5 * ctx->batch; ++i)
     if (!isfinite(out5[i])) return scft_fail(ctx, SCFT_ERR_NOT_FINITE, "free energy is not finite");
   return SCFT_OK;
@@ -377,7 +393,7 @@ void free_all(scft_ctx *ctx) {
   if (ctx->march_exec) cudaGraphExecDestroy(ctx->march_exec);
   ctx->march_exec = nullptr;
   cudaFree(ctx->partial); cudaFree(ctx->sum); cudaFree(ctx->Q); cudaFree(ctx->ffl);
-  cudaFree(ctx->fe5); cudaFree(ctx->tables);
+  cudaFree(ctx->fe5); cudaFree(ctx->tables); cudaFree(ctx->dev_err);
   for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
   ctx->prof_events.clear();
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -441,7 +457,8 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   const scft_params &p = *pin;
   for (int i = 0; i < 7; ++i)
     if (p.reserved[i]) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "reserved fields must be 0");
-  if (p.flags & ~SCFT_FLAG_NO_GRAPH) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad flags");
+  if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_NO_PIPE))
+    return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad flags");
   if (!(p.lx > 0 && p.ly > 0 && p.lz > 0 && p.ds0 > 0 && p.fA >= 0 && p.fA <= 1 && p.batch >= 1))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
   if (p.precision != SCFT_PREC_FP64 && p.precision != SCFT_PREC_FP32)
@@ -479,6 +496,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     return scft_fail(nullptr, st, msg);
   };
   ctx->use_graph = (p.flags & SCFT_FLAG_NO_GRAPH) == 0;
+  ctx->use_pipe = (p.flags & SCFT_FLAG_NO_PIPE) == 0;
   if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
     return fail(SCFT_ERR_CUDA, "stream creation failed");
   if (scft::line_filter_prepare() != cudaSuccess || scft::fast_line_prepare() != cudaSuccess)
@@ -497,7 +515,8 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   ctx->nblk = scft::reduce_blocks(M);
   ok = ok && alloc((void **)&ctx->partial, 8 * B * 3 * ctx->nblk) &&
        alloc((void **)&ctx->sum, 8 * B) && alloc((void **)&ctx->Q, 8 * B) &&
-       alloc((void **)&ctx->ffl, 8 * B) && alloc((void **)&ctx->fe5, 8 * 5 * B);
+       alloc((void **)&ctx->ffl, 8 * B) && alloc((void **)&ctx->fe5, 8 * 5 * B) &&
+       alloc((void **)&ctx->dev_err, sizeof(unsigned));
   if (!ok) {
     cudaGetLastError();
     return fail(SCFT_ERR_NO_MEMORY, "device allocation failed");
@@ -614,8 +633,7 @@ int scft_get_field(scft_ctx *ctx, int field, double *dst) {
   double *d = field_ptr(ctx, field);
   if (!d || !dst) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad field or null pointer");
   CK(cudaMemcpyAsync(dst, d, sizeof(double) * ctx->M * ctx->batch, cudaMemcpyDeviceToHost, ctx->st));
-  CK(cudaStreamSynchronize(ctx->st));
-  return SCFT_OK;
+  return sync_check(ctx);
 }
 
 int scft_average_value(scft_ctx *ctx, int field) {
@@ -727,8 +745,7 @@ int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir) {
 
 int scft_synchronize(scft_ctx *ctx) {
   if (!ctx) return SCFT_ERR_INVALID_ARG;
-  CK(cudaStreamSynchronize(ctx->st));
-  return SCFT_OK;
+  return sync_check(ctx);
 }
 
 long long scft_launch_count(const scft_ctx *ctx) { return ctx ? ctx->launches : -1; }

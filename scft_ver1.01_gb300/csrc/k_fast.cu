@@ -163,6 +163,205 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float
   }
 }
 
+// ------------------------------------------------------------------------
+// The four-step filter core shared by the pipelined kernel: v[j] holds
+// element p + P*j of complex column `lane` on entry and the filtered values
+// on exit.  `after_first_sync` runs once every warp has written its stage-1
+// exchange slots (so every warp has finished reading its inputs).
+template <int N, int P, typename F>
+__device__ __forceinline__ void four_step(float2 (&v)[N / P], float2 *ex, const float2 *tw,
+                                          const float *gain, int p, int lane,
+                                          F &&after_first_sync) {
+  constexpr int R1 = N / P;
+  reg::dft<R1, false>(v);
+  reg::static_for<0, R1>([&](auto k_) {
+    constexpr int k1 = decltype(k_)::value;
+    if (k1 > 0) v[k1] = cmul(v[k1], __ldg(&tw[p * k1]));
+    ex[(k1 * P + p) * 32 + lane] = v[k1];
+  });
+  __syncthreads();
+  after_first_sync();
+  for (int k1 = p; k1 < R1; k1 += P) {
+    float2 u[P];
+    reg::static_for<0, P>([&](auto q_) {
+      constexpr int q = decltype(q_)::value;
+      u[q] = ex[(k1 * P + q) * 32 + lane];
+    });
+    reg::dft<P, false>(u);
+    reg::static_for<0, P>([&](auto k2_) {
+      constexpr int k2 = decltype(k2_)::value;
+      const float g = __ldg(&gain[k1 + R1 * k2]);
+      u[k2].x *= g;
+      u[k2].y *= g;
+    });
+    reg::dft<P, true>(u);
+    reg::static_for<0, P>([&](auto q_) {
+      constexpr int q = decltype(q_)::value;
+      if (q > 0) u[q] = cmul(u[q], cconj(__ldg(&tw[q * k1])));
+      ex[(k1 * P + q) * 32 + lane] = u[q];
+    });
+  }
+  __syncthreads();
+  reg::static_for<0, R1>([&](auto k_) {
+    constexpr int k1 = decltype(k_)::value;
+    v[k1] = ex[(k1 * P + p) * 32 + lane];
+  });
+  reg::dft<R1, true>(v);
+  __syncthreads();   // the exchange buffer is free again
+}
+
+// ---- mbarrier / bulk-copy helpers (bounded waits) ------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// 1-D bulk copy global -> shared (the TMA unit), completing on `bar`.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// Wait for phase `parity` of `bar`, for at most ~1 s of SM clock; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+  const long long t0 = clock64();
+  while (true) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > 2000000000LL) return false;
+  }
+}
+
+// Persistent, pipelined column pass (lines along y or z).  Each CTA loops over
+// tiles (set, instance, outer, 64-wide x-chunk); warp 0 stages the q rows of
+// the next tiles into a two-slot shared-memory ring with cp.async.bulk
+// (256 B per line element, completing on an mbarrier per slot) while all
+// warps filter the current tile in registers.  W is read with plain loads
+// issued before the slot wait.  Output is stored straight from registers.
+template <int N, int P>
+__global__ void __launch_bounds__(P * 32, N <= 128 ? 2 : 1)
+    k_col_pipe(AxisPlan ap, PassSet<float> ps, unsigned *err) {
+  constexpr int R1 = N / P;
+  constexpr unsigned kTileBytes = N * 64 * 4;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float *slot[2] = {reinterpret_cast<float *>(smem_raw),
+                    reinterpret_cast<float *>(smem_raw) + N * 64};
+  float2 *ex = reinterpret_cast<float2 *>(smem_raw + 2 * kTileBytes);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + 3 * kTileBytes);
+  const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
+  const int ntx = ap.n_real / 64;
+  const long long T = (long long)ps.nset * ps.batch * ap.n_outer * ntx;
+  const float2 *__restrict__ tw = reinterpret_cast<const float2 *>(ap.twiddle);
+  const float *__restrict__ gain = reinterpret_cast<const float *>(ap.gain);
+
+  struct Tile {
+    const float *in;
+    float *out;
+    const float *w;     // W at this tile (pre or post), or null
+    bool pre;
+  };
+  auto tile_of = [&](long long t) {
+    const int xt = (int)(t % ntx);
+    long long r = t / ntx;
+    const int outer = (int)(r % ap.n_outer);
+    r /= ap.n_outer;
+    const long long b = r % ps.batch;
+    const int set = (int)(r / ps.batch);
+    const long long off = (long long)outer * ap.s_outer + (long long)xt * 64;
+    Tile tl;
+    tl.in = (set ? ps.in[1] : ps.in[0]) + b * (set ? ps.in_bs[1] : ps.in_bs[0]) + off;
+    tl.out = (set ? ps.out[1] : ps.out[0]) + b * (set ? ps.out_bs[1] : ps.out_bs[0]) + off;
+    const float *pre = set ? ps.pre[1] : ps.pre[0];
+    const float *post = set ? ps.post[1] : ps.post[0];
+    tl.pre = pre != nullptr;
+    tl.w = pre ? pre + b * ps.w_bs + off : (post ? post + b * ps.w_bs + off : nullptr);
+    return tl;
+  };
+  // warp 0: stage tile t into slot s
+  auto issue = [&](long long t, int s) {
+    if (p != 0 || t >= T) return;
+    const Tile tl = tile_of(t);
+    if (lane == 0) mbar_expect_tx(&bar[s], kTileBytes);
+    __syncwarp();
+#pragma unroll
+    for (int n = lane; n < N; n += 32)
+      bulk_g2s(slot[s] + n * 64, tl.in + (long long)n * ap.s_n, 256, &bar[s]);
+  };
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  pdl_wait();      // inputs are the previous pass's output
+  pdl_release();
+  long long t = blockIdx.x;
+  issue(t, 0);
+  issue(t + gridDim.x, 1);
+  for (int it = 0; t < T; ++it, t += gridDim.x) {
+    const int s = it & 1;
+    const unsigned parity = (it >> 1) & 1;
+    const Tile tl = tile_of(t);
+    float2 wv[R1];
+    if (tl.w && tl.pre) {
+      reg::static_for<0, R1>([&](auto j_) {
+        constexpr int j = decltype(j_)::value;
+        wv[j] = __ldg(reinterpret_cast<const float2 *>(tl.w + (long long)(p + P * j) * ap.s_n +
+                                                        2 * lane));
+      });
+    }
+    // block-uniform give-up: every thread leaves together, none is left at a barrier
+    if (!__syncthreads_and(mbar_wait(&bar[s], parity) ? 1 : 0)) {
+      if (threadIdx.x == 0) atomicOr(err, 1u);
+      return;
+    }
+    float2 v[R1];
+    reg::static_for<0, R1>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      v[j] = reinterpret_cast<const float2 *>(slot[s] + (p + P * j) * 64)[lane];
+      if (tl.w && tl.pre) {
+        v[j].x *= wv[j].x;
+        v[j].y *= wv[j].y;
+      }
+    });
+    four_step<N, P>(v, ex, tw, gain, p, lane, [&]() {
+      // every warp has read slot s: refill it with the tile after next
+      if (p == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(t + 2LL * gridDim.x, s);
+    });
+    reg::static_for<0, R1>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      const long long off = (long long)(p + P * j) * ap.s_n + 2 * lane;
+      float2 r = v[j];
+      if (tl.w && !tl.pre) {
+        const float2 w = __ldg(reinterpret_cast<const float2 *>(tl.w + off));
+        r.x *= w.x;
+        r.y *= w.y;
+      }
+      *reinterpret_cast<float2 *>(tl.out + off) = r;
+    });
+  }
+}
+
+template <int N, int P> size_t pipe_smem() { return (size_t)3 * N * 64 * 4 + 16; }
+
 template <int N, int P, bool XP> size_t fast_smem() {
   const size_t ex = (size_t)N * 32 * sizeof(float2);
   const size_t stg = XP ? (size_t)64 * (N + 1) * sizeof(float) : 0;
@@ -187,6 +386,38 @@ bool fast_line_supported(const AxisPlan &ap) {
   return ap.n_real % 64 == 0;
 }
 
+namespace {
+constexpr int kMaxDev = 64;
+int g_pipe_grid[kMaxDev][4];   // persistent grid size per device and N index (0: not set up)
+
+template <int N, int P> cudaError_t prep_pipe(int dev, int idx) {
+  cudaError_t e = cudaFuncSetAttribute(k_col_pipe<N, P>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)pipe_smem<N, P>());
+  if (e != cudaSuccess) return e;
+  int per_sm = 0, nsm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_col_pipe<N, P>, P * 32,
+                                                    pipe_smem<N, P>());
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  g_pipe_grid[dev][idx] = (per_sm > 0 ? per_sm : 1) * nsm;
+  return cudaSuccess;
+}
+
+template <int N, int P>
+cudaError_t launch_pipe(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st, int idx) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const long long T = (long long)ps.nset * ps.batch * ap.n_outer * (ap.n_real / 64);
+  long long g = g_pipe_grid[dev][idx];
+  if (g <= 0) return cudaErrorInitializationError;
+  if (g > T) g = T;
+  return launch_pdl(k_col_pipe<N, P>, dim3((unsigned)g), dim3(P * 32), pipe_smem<N, P>(), st, ap,
+                    ps, ps.err);
+}
+}  // namespace
+
 cudaError_t fast_line_prepare() {
   cudaError_t e = cudaSuccess;
 #define PREP(N, P)                                              \
@@ -197,12 +428,30 @@ cudaError_t fast_line_prepare() {
   PREP(128, 8)
   PREP(256, 16)
 #undef PREP
+  int dev = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+  if ((e = prep_pipe<32, 4>(dev, 0)) != cudaSuccess) return e;
+  if ((e = prep_pipe<64, 8>(dev, 1)) != cudaSuccess) return e;
+  if ((e = prep_pipe<128, 8>(dev, 2)) != cudaSuccess) return e;
+  if ((e = prep_pipe<256, 16>(dev, 3)) != cudaSuccess) return e;
   return e;
 }
 
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
   if (ps.nset < 1 || ps.nset > kMaxSet) return cudaErrorInvalidValue;
   const bool xp = ap.n_fast != 0;
+  // column passes: the persistent pipelined kernel when the caller supplied
+  // an error word for its bounded waits
+  if (!xp && ps.err) {
+    switch (ap.n) {
+      case 32: return launch_pipe<32, 4>(ap, ps, st, 0);
+      case 64: return launch_pipe<64, 8>(ap, ps, st, 1);
+      case 128: return launch_pipe<128, 8>(ap, ps, st, 2);
+      case 256: return launch_pipe<256, 16>(ap, ps, st, 3);
+      default: break;
+    }
+  }
   switch (ap.n) {
     case 32: return xp ? launch_one<32, 4, true>(ap, ps, st) : launch_one<32, 4, false>(ap, ps, st);
     case 64: return xp ? launch_one<64, 8, true>(ap, ps, st) : launch_one<64, 8, false>(ap, ps, st);

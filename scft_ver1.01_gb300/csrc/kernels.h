@@ -40,6 +40,7 @@ template <typename R> struct PassSet {
   long long w_bs;
   int nset;
   int batch;
+  unsigned *err;   // device error word (bounded-wait timeouts), may be null for non-pipelined kernels
 };
 
 // Register-resident FP32 pass (k_fast.cu): n in {32, 64, 128, 256} and
