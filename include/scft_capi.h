@@ -78,7 +78,8 @@ typedef struct scft_params {
 
 /* flags */
 #define SCFT_FLAG_NO_GRAPH 1      /* issue the march phase as plain launches, not a CUDA graph */
-#define SCFT_FLAG_NO_PIPE 2       /* one-tile-per-CTA column passes instead of the persistent pipelined kernel */
+#define SCFT_FLAG_PIPE 2          /* persistent column passes with a cp.async.bulk staging ring
+                                     (slower than the default one-tile-per-CTA kernel at 128^3) */
 
 /* Fill *p with the reference defaults (32^3, box 4, xN 20, fa 0.5,
  * ds0 0.01, batch 1, FP64, simple mixing wopt 0.05 wcmp 0.10). */

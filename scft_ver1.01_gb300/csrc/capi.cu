@@ -457,7 +457,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   const scft_params &p = *pin;
   for (int i = 0; i < 7; ++i)
     if (p.reserved[i]) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "reserved fields must be 0");
-  if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_NO_PIPE))
+  if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_PIPE))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad flags");
   if (!(p.lx > 0 && p.ly > 0 && p.lz > 0 && p.ds0 > 0 && p.fA >= 0 && p.fA <= 1 && p.batch >= 1))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
@@ -496,7 +496,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     return scft_fail(nullptr, st, msg);
   };
   ctx->use_graph = (p.flags & SCFT_FLAG_NO_GRAPH) == 0;
-  ctx->use_pipe = (p.flags & SCFT_FLAG_NO_PIPE) == 0;
+  ctx->use_pipe = (p.flags & SCFT_FLAG_PIPE) != 0;
   if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
     return fail(SCFT_ERR_CUDA, "stream creation failed");
   if (scft::line_filter_prepare() != cudaSuccess || scft::fast_line_prepare() != cudaSuccess)

@@ -17,7 +17,7 @@ struct scft_ctx {
   int rbytes = 8;               // sizeof working real (4 or 8)
   cudaStream_t st = nullptr;    // the context's stream (every launch)
   bool use_graph = true;        // march phase replayed as a CUDA graph
-  bool use_pipe = true;         // persistent pipelined column passes
+  bool use_pipe = false;        // persistent pipelined column passes (opt-in)
   unsigned *dev_err = nullptr;  // device error word (bounded-wait timeouts)
   cudaGraphExec_t march_exec = nullptr;
   long long march_nodes = 0;    // kernel launches inside the graph
