@@ -23,6 +23,14 @@ namespace scft {
 
 namespace {
 
+// Shared memory of k_fast_line before its tables: the exchange buffer
+// (N x 32 complex), or the 64-row staging tile (pitch N+1) of the x pass.
+template <int N, bool XP> __host__ __device__ constexpr size_t fast_core_smem() {
+  return ((size_t)N * 32 * 8 > (XP ? (size_t)64 * (N + 1) * 4 : 0))
+             ? (size_t)N * 32 * 8
+             : (((size_t)64 * (N + 1) * 4 + 15) / 16) * 16;
+}
+
 template <int N, int P, bool XP>
 __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float> ps) {
   constexpr int R1 = N / P;
@@ -40,11 +48,20 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float
   const long long in_bs = set ? ps.in_bs[1] : ps.in_bs[0];
   const long long out_bs = set ? ps.out_bs[1] : ps.out_bs[0];
   const long long w_bs = ps.w_bs;
+  // The twiddle and gain tables go to shared memory first: they do not depend
+  // on the previous pass, so this overlaps its tail, and the FFT stages then
+  // read them with shared-memory broadcasts instead of dependent global loads.
+  float2 *s_tw = reinterpret_cast<float2 *>(smem_raw + fast_core_smem<N, XP>());
+  float *s_g = reinterpret_cast<float *>(s_tw + N);
+  for (int i = threadIdx.x; i < N; i += NT) {
+    s_tw[i] = __ldg(reinterpret_cast<const float2 *>(ap.twiddle) + i);
+    s_g[i] = __ldg(reinterpret_cast<const float *>(ap.gain) + i);
+  }
   // the input slice is the previous pass's output
   pdl_wait();
   pdl_release();
-  const float2 *__restrict__ tw = reinterpret_cast<const float2 *>(ap.twiddle);
-  const float *__restrict__ gain = reinterpret_cast<const float *>(ap.gain);
+  const float2 *tw = s_tw;
+  const float *gain = s_g;
   float2 v[R1];
   long long base;
 
@@ -54,7 +71,7 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float
     base = (long long)blockIdx.x * 64 * N;  // 64 consecutive rows of N floats
     const float *src = in + b * in_bs + base;
     const float *wsrc = pre ? pre + b * w_bs + base : nullptr;
-#pragma unroll 4
+#pragma unroll
     for (int i = threadIdx.x; i < 64 * N; i += NT) {
       const int r = i / N, c = i % N;
       float x = __ldg(src + i);
@@ -85,13 +102,14 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float
         v[j].y *= w.y;
       });
     }
+    __syncthreads();   // the shared tables are complete
   }
 
   // ---- stage 1: DFT_R1 over j, twiddle, exchange
   reg::dft<R1, false>(v);
   reg::static_for<0, R1>([&](auto k_) {
     constexpr int k1 = decltype(k_)::value;
-    if (k1 > 0) v[k1] = cmul(v[k1], __ldg(&tw[p * k1]));
+    if (k1 > 0) v[k1] = cmul(v[k1], tw[p * k1]);
     ex[(k1 * P + p) * 32 + lane] = v[k1];
   });
   __syncthreads();
@@ -106,14 +124,14 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float
     reg::dft<P, false>(u);
     reg::static_for<0, P>([&](auto k2_) {
       constexpr int k2 = decltype(k2_)::value;
-      const float g = __ldg(&gain[k1 + R1 * k2]);
+      const float g = gain[k1 + R1 * k2];
       u[k2].x *= g;
       u[k2].y *= g;
     });
     reg::dft<P, true>(u);
     reg::static_for<0, P>([&](auto q_) {
       constexpr int q = decltype(q_)::value;
-      if (q > 0) u[q] = cmul(u[q], cconj(__ldg(&tw[q * k1])));
+      if (q > 0) u[q] = cmul(u[q], cconj(tw[q * k1]));
       ex[(k1 * P + q) * 32 + lane] = u[q];
     });
   }
@@ -176,7 +194,7 @@ __device__ __forceinline__ void four_step(float2 (&v)[N / P], float2 *ex, const 
   reg::dft<R1, false>(v);
   reg::static_for<0, R1>([&](auto k_) {
     constexpr int k1 = decltype(k_)::value;
-    if (k1 > 0) v[k1] = cmul(v[k1], __ldg(&tw[p * k1]));
+    if (k1 > 0) v[k1] = cmul(v[k1], tw[p * k1]);
     ex[(k1 * P + p) * 32 + lane] = v[k1];
   });
   __syncthreads();
@@ -190,14 +208,14 @@ __device__ __forceinline__ void four_step(float2 (&v)[N / P], float2 *ex, const 
     reg::dft<P, false>(u);
     reg::static_for<0, P>([&](auto k2_) {
       constexpr int k2 = decltype(k2_)::value;
-      const float g = __ldg(&gain[k1 + R1 * k2]);
+      const float g = gain[k1 + R1 * k2];
       u[k2].x *= g;
       u[k2].y *= g;
     });
     reg::dft<P, true>(u);
     reg::static_for<0, P>([&](auto q_) {
       constexpr int q = decltype(q_)::value;
-      if (q > 0) u[q] = cmul(u[q], cconj(__ldg(&tw[q * k1])));
+      if (q > 0) u[q] = cmul(u[q], cconj(tw[q * k1]));
       ex[(k1 * P + q) * 32 + lane] = u[q];
     });
   }
@@ -363,9 +381,7 @@ __global__ void __launch_bounds__(P * 32, N <= 128 ? 2 : 1)
 template <int N, int P> size_t pipe_smem() { return (size_t)3 * N * 64 * 4 + 16; }
 
 template <int N, int P, bool XP> size_t fast_smem() {
-  const size_t ex = (size_t)N * 32 * sizeof(float2);
-  const size_t stg = XP ? (size_t)64 * (N + 1) * sizeof(float) : 0;
-  return ex > stg ? ex : stg;
+  return fast_core_smem<N, XP>() + (size_t)N * (sizeof(float2) + sizeof(float));
 }
 
 template <int N, int P, bool XP>
