@@ -13,9 +13,9 @@
 
 #include <string>
 
-#include "../../include/compat/cuda_scft.h"
-#include "../../include/compat/init.h"
-#include "../../include/compat/init_cuda.h"
+#include "compat/cuda_scft.h"
+#include "compat/init.h"
+#include "compat/init_cuda.h"
 #include "ctx.h"
 
 namespace {

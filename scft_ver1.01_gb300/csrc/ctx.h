@@ -6,7 +6,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/scft_capi.h"
+#include "scft_capi.h"
 #include "kernels.h"
 
 struct scft_ctx {

@@ -35,7 +35,7 @@ template <int N, int P, bool XP>
 __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float> ps) {
   constexpr int R1 = N / P;
   constexpr int NT = P * 32;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   float2 *ex = reinterpret_cast<float2 *>(smem_raw);
   const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
   // blockIdx.z = set * batch + instance
