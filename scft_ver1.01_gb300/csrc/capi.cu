@@ -115,7 +115,7 @@ int seg_boundary(scft_ctx *ctx, const Seg &s, cudaStream_t st) {
 // independent, so the interleaving does not change any result.
 template <typename R>
 int run_chains(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nchain,
-               cudaStream_t st) {
+               cudaStream_t st, int chain_base) {
   const long long M = ctx->M;
   int total[scft::kMaxSet] = {0, 0};
   int maxT = 0;
@@ -149,7 +149,7 @@ int run_chains(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nch
       q_dst[nact] = q + (long long)dst * M;
       q_src[nact] = q + (long long)src * M;
       W[nact] = static_cast<const R *>(ctx->W[s.wf]);
-      cidx[nact] = c;
+      cidx[nact] = c + chain_base;   // selects the chain's intermediates
       ++nact;
     }
     for (int pi = 0; pi < np; ++pi) {
@@ -177,9 +177,9 @@ int run_chains(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nch
 }
 
 int run_chains_any(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nchain,
-                   cudaStream_t st) {
-  return ctx->rbytes == 4 ? run_chains<float>(ctx, chains, nseg, nchain, st)
-                          : run_chains<double>(ctx, chains, nseg, nchain, st);
+                   cudaStream_t st, int chain_base = 0) {
+  return ctx->rbytes == 4 ? run_chains<float>(ctx, chains, nseg, nchain, st, chain_base)
+                          : run_chains<double>(ctx, chains, nseg, nchain, st, chain_base);
 }
 
 // initilize_wdz (cuda_scft.cu:450) for field f into W[f].
@@ -204,7 +204,16 @@ int march_phase(scft_ctx *ctx, cudaStream_t st) {
                      {SCFT_Q_CA, SCFT_FIELD_WA, SCFT_Q_CB, 0, ctx->NsA, -1}};
   const Seg *chains[2] = {c0, c1};
   const int nseg[2] = {2, 2};
-  return run_chains_any(ctx, chains, nseg, 2, st);
+  if (!ctx->two_streams) return run_chains_any(ctx, chains, nseg, 2, st);
+  // the chains on two forked streams: each pass launch of one chain can fill
+  // the SMs left idle by the tail of the other chain's launch
+  CK(cudaEventRecord(ctx->ev_fork, st));
+  CK(cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0));
+  int rc = run_chains_any(ctx, &chains[0], &nseg[0], 1, st, 0);
+  if (!rc) rc = run_chains_any(ctx, &chains[1], &nseg[1], 1, ctx->st2, 1);
+  CK(cudaEventRecord(ctx->ev_join, ctx->st2));
+  CK(cudaStreamWaitEvent(st, ctx->ev_join, 0));
+  return rc;
 }
 
 // The march phase through a CUDA graph captured on first use (the pointers
@@ -392,6 +401,9 @@ void free_all(scft_ctx *ctx) {
   for (int i = 0; i < 4; ++i) cudaFree(ctx->tmp[i]);
   if (ctx->march_exec) cudaGraphExecDestroy(ctx->march_exec);
   ctx->march_exec = nullptr;
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->st2) cudaStreamDestroy(ctx->st2);
   cudaFree(ctx->partial); cudaFree(ctx->sum); cudaFree(ctx->Q); cudaFree(ctx->ffl);
   cudaFree(ctx->fe5); cudaFree(ctx->tables); cudaFree(ctx->dev_err);
   for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
@@ -457,7 +469,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   const scft_params &p = *pin;
   for (int i = 0; i < 7; ++i)
     if (p.reserved[i]) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "reserved fields must be 0");
-  if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_PIPE))
+  if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_PIPE | SCFT_FLAG_TWO_STREAMS))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad flags");
   if (!(p.lx > 0 && p.ly > 0 && p.lz > 0 && p.ds0 > 0 && p.fA >= 0 && p.fA <= 1 && p.batch >= 1))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
@@ -497,7 +509,11 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   };
   ctx->use_graph = (p.flags & SCFT_FLAG_NO_GRAPH) == 0;
   ctx->use_pipe = (p.flags & SCFT_FLAG_PIPE) != 0;
-  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
+  ctx->two_streams = (p.flags & SCFT_FLAG_TWO_STREAMS) != 0;
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
     return fail(SCFT_ERR_CUDA, "stream creation failed");
   if (scft::line_filter_prepare() != cudaSuccess || scft::fast_line_prepare() != cudaSuccess)
     return fail(SCFT_ERR_CUDA, "kernel attribute set-up failed");

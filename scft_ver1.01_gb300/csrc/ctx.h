@@ -18,6 +18,9 @@ struct scft_ctx {
   cudaStream_t st = nullptr;    // the context's stream (every launch)
   bool use_graph = true;        // march phase replayed as a CUDA graph
   bool use_pipe = false;        // persistent pipelined column passes (opt-in)
+  bool two_streams = false;     // march chains on two forked streams instead of lockstep
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   unsigned *dev_err = nullptr;  // device error word (bounded-wait timeouts)
   cudaGraphExec_t march_exec = nullptr;
   long long march_nodes = 0;    // kernel launches inside the graph
