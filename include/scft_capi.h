@@ -80,7 +80,8 @@ typedef struct scft_params {
 #define SCFT_FLAG_NO_GRAPH 1      /* issue the march phase as plain launches, not a CUDA graph */
 #define SCFT_FLAG_PIPE 2          /* persistent column passes with a cp.async.bulk staging ring
                                      (slower than the default one-tile-per-CTA kernel at 128^3) */
-#define SCFT_FLAG_TWO_STREAMS 4   /* march chains on two forked streams instead of shared lockstep launches */
+#define SCFT_FLAG_TWO_STREAMS 4   /* march chains on two forked streams (default when batch*M >= 2^20) */
+#define SCFT_FLAG_LOCKSTEP 8      /* march chains in shared lockstep launches (default below 2^20 points) */
 
 /* Fill *p with the reference defaults (32^3, box 4, xN 20, fa 0.5,
  * ds0 0.01, batch 1, FP64, simple mixing wopt 0.05 wcmp 0.10). */
