@@ -82,6 +82,7 @@ typedef struct scft_params {
                                      (slower than the default one-tile-per-CTA kernel at 128^3) */
 #define SCFT_FLAG_TWO_STREAMS 4   /* march chains on two forked streams (default when batch*M >= 2^20) */
 #define SCFT_FLAG_LOCKSTEP 8      /* march chains in shared lockstep launches (default below 2^20 points) */
+#define SCFT_FLAG_NO_XY 16        /* separate x and y passes instead of the fused plane kernel */
 
 /* Fill *p with the reference defaults (32^3, box 4, xN 20, fa 0.5,
  * ds0 0.01, batch 1, FP64, simple mixing wopt 0.05 wcmp 0.10). */

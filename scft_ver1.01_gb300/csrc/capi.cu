@@ -125,7 +125,10 @@ int run_chains(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nch
     int rc = seg_boundary<R>(ctx, chains[c][0], st);
     if (rc) return rc;
   }
-  const int np = (int)ctx->passes.size();
+  // stages per step: the x and y passes fused into one plane kernel when
+  // possible (FP32), then the remaining passes
+  const bool xy = sizeof(R) == 4 && ctx->fuse_xy;
+  const int np = (int)ctx->passes.size() - (xy ? 1 : 0);
   for (int t = 1; t <= maxT; ++t) {
     scft::PassSet<R> ps[3];
     int nact = 0;
@@ -169,7 +172,14 @@ int run_chains(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nch
         p.pre[a] = pi == 0 ? W[a] : nullptr;
         p.post[a] = pi == np - 1 ? W[a] : nullptr;
       }
-      int rc = launch_set<R>(ctx, ctx->passes[pi], p, st);
+      int rc;
+      if constexpr (sizeof(R) == 4) {
+        if (xy && pi == 0) {
+          CKL(scft::launch_xy(ctx->passes[0], ctx->passes[1], p, st));
+          continue;
+        }
+      }
+      rc = launch_set<R>(ctx, ctx->passes[xy ? pi + 1 : pi], p, st);
       if (rc) return rc;
     }
   }
@@ -469,7 +479,8 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   const scft_params &p = *pin;
   for (int i = 0; i < 7; ++i)
     if (p.reserved[i]) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "reserved fields must be 0");
-  if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_PIPE | SCFT_FLAG_TWO_STREAMS | SCFT_FLAG_LOCKSTEP))
+  if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_PIPE | SCFT_FLAG_TWO_STREAMS |
+                  SCFT_FLAG_LOCKSTEP | SCFT_FLAG_NO_XY))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad flags");
   if (!(p.lx > 0 && p.ly > 0 && p.lz > 0 && p.ds0 > 0 && p.fA >= 0 && p.fA <= 1 && p.batch >= 1))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
@@ -606,6 +617,11 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     off = (off + 255) & ~(size_t)255;
     ctx->passes.push_back(ap);
   }
+  // x and y both as their own passes (no length-1 axis among them) and small
+  // enough for a shared-memory plane: fuse them
+  ctx->fuse_xy = rb == 4 && (p.flags & SCFT_FLAG_NO_XY) == 0 && ctx->passes.size() >= 2 &&
+                 axes[0] == 0 && axes[1] == 1 &&
+                 scft::xy_fusable(ctx->passes[0], ctx->passes[1]);
   if (cudaMemcpy(ctx->tables, host.data(), tab_bytes, cudaMemcpyHostToDevice) != cudaSuccess)
     return fail(SCFT_ERR_CUDA, "table upload failed");
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(SCFT_ERR_CUDA, "set-up failed");

@@ -19,6 +19,7 @@ struct scft_ctx {
   bool use_graph = true;        // march phase replayed as a CUDA graph
   bool use_pipe = false;        // persistent pipelined column passes (opt-in)
   bool two_streams = false;     // march chains on two forked streams instead of lockstep
+  bool fuse_xy = false;         // x and y passes fused into one plane kernel (FP32)
   cudaStream_t st2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   unsigned *dev_err = nullptr;  // device error word (bounded-wait timeouts)

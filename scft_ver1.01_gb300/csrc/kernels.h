@@ -46,6 +46,10 @@ template <typename R> struct PassSet {
 // Register-resident FP32 pass (k_fast.cu): n in {32, 64, 128, 256} and
 // n_real a multiple of 64.
 bool fast_line_supported(const AxisPlan &ap);
+// Fused x+y pass over whole z-planes (k_fast.cu): Nx, Ny in {64, 128}.
+bool xy_fusable(const AxisPlan &apx, const AxisPlan &apy);
+cudaError_t launch_xy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
+                      cudaStream_t st);
 cudaError_t fast_line_prepare();
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
 
