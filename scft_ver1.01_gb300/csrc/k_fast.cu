@@ -186,9 +186,17 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float
 // element p + P*j of complex column `lane` on entry and the filtered values
 // on exit.  `after_first_sync` runs once every warp has written its stage-1
 // exchange slots (so every warp has finished reading its inputs).
+// bar_id 0 synchronises the whole CTA; bar_id > 0 only the P warps of one
+// warp group (named barrier bar_id), so several groups can filter
+// independent line sets in one CTA.
+__device__ __forceinline__ void group_sync(int bar_id, int nthreads) {
+  if (bar_id == 0) __syncthreads();
+  else asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(nthreads) : "memory");
+}
+
 template <int N, int P, typename F>
 __device__ __forceinline__ void four_step(float2 (&v)[N / P], float2 *ex, const float2 *tw,
-                                          const float *gain, int p, int lane,
+                                          const float *gain, int p, int lane, int bar_id,
                                           F &&after_first_sync) {
   constexpr int R1 = N / P;
   reg::dft<R1, false>(v);
@@ -197,7 +205,7 @@ __device__ __forceinline__ void four_step(float2 (&v)[N / P], float2 *ex, const 
     if (k1 > 0) v[k1] = cmul(v[k1], tw[p * k1]);
     ex[(k1 * P + p) * 32 + lane] = v[k1];
   });
-  __syncthreads();
+  group_sync(bar_id, P * 32);
   after_first_sync();
   for (int k1 = p; k1 < R1; k1 += P) {
     float2 u[P];
@@ -219,13 +227,13 @@ __device__ __forceinline__ void four_step(float2 (&v)[N / P], float2 *ex, const 
       ex[(k1 * P + q) * 32 + lane] = u[q];
     });
   }
-  __syncthreads();
+  group_sync(bar_id, P * 32);
   reg::static_for<0, R1>([&](auto k_) {
     constexpr int k1 = decltype(k_)::value;
     v[k1] = ex[(k1 * P + p) * 32 + lane];
   });
   reg::dft<R1, true>(v);
-  __syncthreads();   // the exchange buffer is free again
+  group_sync(bar_id, P * 32);   // the exchange buffer is free again
 }
 
 // ---- mbarrier / bulk-copy helpers (bounded waits) ------------------------
@@ -359,7 +367,7 @@ __global__ void __launch_bounds__(P * 32, N <= 128 ? 2 : 1)
         v[j].y *= wv[j].y;
       }
     });
-    four_step<N, P>(v, ex, tw, gain, p, lane, [&]() {
+    four_step<N, P>(v, ex, tw, gain, p, lane, 0, [&]() {
       // every warp has read slot s: refill it with the tile after next
       if (p == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       issue(t + 2LL * gridDim.x, s);
@@ -390,23 +398,29 @@ template <int N, int P> size_t pipe_smem() { return (size_t)3 * N * 64 * 4 + 16;
 template <int NX, int NY> constexpr size_t xy_plane_bytes() {
   return (((size_t)NY * (NX + 1) * 4 + 127) / 128) * 128;
 }
-template <int NX, int NY> constexpr size_t xy_smem() {
-  return xy_plane_bytes<NX, NY>() + (size_t)(NX > NY ? NX : NY) * 32 * 8 +
+// G warp groups of 8 warps: group g takes rounds g, g+G, ... of each pass with
+// its own exchange buffer and named barrier, so G groups keep G planes' worth
+// of independent work in flight per plane.
+template <int NX, int NY, int G> constexpr size_t xy_smem() {
+  return xy_plane_bytes<NX, NY>() + (size_t)G * (NX > NY ? NX : NY) * 32 * 8 +
          (size_t)(NX + NY) * 12;
 }
 
-template <int NX, int NY>
-__global__ void __launch_bounds__(256, 2) k_xy_plane(AxisPlan apx, AxisPlan apy,
-                                                     PassSet<float> ps) {
-  constexpr int P = 8, NT = 256, PITCH = NX + 1;
+template <int NX, int NY, int G>
+__global__ void __launch_bounds__(256 * G, G == 1 ? 2 : 1)
+    k_xy_plane(AxisPlan apx, AxisPlan apy, PassSet<float> ps) {
+  constexpr int P = 8, NT = 256 * G, PITCH = NX + 1;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float *plane = reinterpret_cast<float *>(smem_raw);
-  float2 *ex = reinterpret_cast<float2 *>(smem_raw + xy_plane_bytes<NX, NY>());
-  float2 *twx = ex + (NX > NY ? NX : NY) * 32;
+  const int grp = G == 1 ? 0 : (int)(threadIdx.x >> 8);
+  float2 *ex0 = reinterpret_cast<float2 *>(smem_raw + xy_plane_bytes<NX, NY>());
+  float2 *ex = ex0 + grp * (NX > NY ? NX : NY) * 32;
+  float2 *twx = ex0 + G * (NX > NY ? NX : NY) * 32;
   float2 *twy = twx + NX;
   float *gx = reinterpret_cast<float *>(twy + NY);
   float *gy = gx + NX;
-  const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, p = (threadIdx.x >> 5) & 7;
+  const int bar_id = G == 1 ? 0 : 1 + grp;
   const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
   const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
   const long long base = (long long)blockIdx.x * NX * NY;
@@ -435,7 +449,7 @@ __global__ void __launch_bounds__(256, 2) k_xy_plane(AxisPlan apx, AxisPlan apy,
   __syncthreads();
   // x pass, NY/64 rounds of 32 complex rows
 #pragma unroll 1
-  for (int r = 0; r < NY / 64; ++r) {
+  for (int r = grp; r < NY / 64; r += G) {
     float2 v[NX / P];
     const int ra = r * 32 + lane, rb = ra + NY / 2;
     reg::static_for<0, NX / P>([&](auto j_) {
@@ -443,7 +457,7 @@ __global__ void __launch_bounds__(256, 2) k_xy_plane(AxisPlan apx, AxisPlan apy,
       const int n = p + P * j;
       v[j] = make_float2(plane[ra * PITCH + n], plane[rb * PITCH + n]);
     });
-    four_step<NX, P>(v, ex, twx, gx, p, lane, []() {});
+    four_step<NX, P>(v, ex, twx, gx, p, lane, bar_id, []() {});
     reg::static_for<0, NX / P>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
       const int n = p + P * j;
@@ -454,7 +468,7 @@ __global__ void __launch_bounds__(256, 2) k_xy_plane(AxisPlan apx, AxisPlan apy,
   __syncthreads();
   // y pass, NX/64 rounds of 32 complex columns, stored to global
 #pragma unroll 1
-  for (int r = 0; r < NX / 64; ++r) {
+  for (int r = grp; r < NX / 64; r += G) {
     float2 v[NY / P];
     const int ca = r * 64 + lane, cb = ca + 32;
     reg::static_for<0, NY / P>([&](auto j_) {
@@ -462,7 +476,7 @@ __global__ void __launch_bounds__(256, 2) k_xy_plane(AxisPlan apx, AxisPlan apy,
       const int n = p + P * j;
       v[j] = make_float2(plane[n * PITCH + ca], plane[n * PITCH + cb]);
     });
-    four_step<NY, P>(v, ex, twy, gy, p, lane, []() {});
+    four_step<NY, P>(v, ex, twy, gy, p, lane, bar_id, []() {});
     reg::static_for<0, NY / P>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
       const int n = p + P * j;
@@ -529,15 +543,21 @@ cudaError_t launch_pipe(const AxisPlan &ap, const PassSet<float> &ps, cudaStream
   return launch_pdl(k_col_pipe<N, P>, dim3((unsigned)g), dim3(P * 32), pipe_smem<N, P>(), st, ap,
                     ps, ps.err);
 }
+// two warp groups when both passes have two rounds (128 x 128 planes)
+template <int NX, int NY> constexpr int xy_groups() { return (NX >= 128 && NY >= 128) ? 2 : 1; }
+
 template <int NX, int NY> cudaError_t prep_xy() {
-  return cudaFuncSetAttribute(k_xy_plane<NX, NY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)xy_smem<NX, NY>());
+  constexpr int G = xy_groups<NX, NY>();
+  return cudaFuncSetAttribute(k_xy_plane<NX, NY, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)xy_smem<NX, NY, G>());
 }
 template <int NX, int NY>
 cudaError_t launch_xy_t(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
                         cudaStream_t st) {
+  constexpr int G = xy_groups<NX, NY>();
   dim3 grid(apy.n_outer, 1, ps.nset * ps.batch);   // one CTA per z-plane
-  return launch_pdl(k_xy_plane<NX, NY>, grid, dim3(256), xy_smem<NX, NY>(), st, apx, apy, ps);
+  return launch_pdl(k_xy_plane<NX, NY, G>, grid, dim3(256 * G), xy_smem<NX, NY, G>(), st, apx,
+                    apy, ps);
 }
 }  // namespace
 
