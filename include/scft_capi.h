@@ -69,11 +69,12 @@ typedef struct scft_params {
   double wopt;              /* simple-mixing step, reference 0.05 */
   double wcmp;              /* incompressibility weight, reference 0.10 */
   int mixing;               /* SCFT_MIX_* */
-  int anderson_history;     /* Anderson history length (e.g. 20) */
-  double anderson_lambda;   /* Anderson step on the residual */
+  int anderson_history;     /* Anderson history length m (1..32, e.g. 20) */
+  double anderson_lambda;   /* Anderson step on the mixed residual */
   int device;               /* CUDA device ordinal */
   int flags;                /* SCFT_FLAG_* */
-  int reserved[7];          /* must be zero */
+  double anderson_start;    /* simple mixing until the residual max-norm drops below this */
+  int reserved[5];          /* must be zero */
 } scft_params;
 
 /* flags */
@@ -163,6 +164,28 @@ int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir);
 
 /* Wait for all work queued on the context's stream. */
 int scft_synchronize(scft_ctx *ctx);
+
+/* ---- convergence (no reference counterpart: the reference always runs
+ * MaxIT iterations, cuda_scft.cu:253) ----
+ * The residual is phi_w's update direction before the wopt step
+ * (cuda_aid.cu:398-408): dA = xN phB + eta - wA - wcmp(1-phA-phB), dB likewise.
+ * After each iteration the context holds err_max = max_r max(|dA|,|dB|) and
+ * err_rms = sqrt(<dA^2+dB^2>/2), per instance. */
+int scft_get_residual(scft_ctx *ctx, double *err_max, double *err_rms);
+
+/* Iterate until every instance has err_max < tol or max_it iterations ran.
+ * Mixing follows params.mixing: SCFT_MIX_SIMPLE is the reference's phi_w;
+ * SCFT_MIX_ANDERSON uses simple mixing until err_max < anderson_start, then
+ * Anderson mixing over the last anderson_history residuals (Gram matrix and
+ * least squares in FP64, solved on the device).  *iters receives the
+ * iterations run; out5 (batch*5 doubles, may be NULL) the free energy after
+ * the last one.  Returns SCFT_ERR_NOT_FINITE on divergence. */
+int scft_converge(scft_ctx *ctx, double tol, int max_it, int *iters, double *out5);
+
+/* Device-to-device copy of wa, wb, pha, phb from src to dst (same grid and
+ * batch; the contexts may differ in precision).  Used for an FP64 polish of
+ * an FP32 solve. */
+int scft_copy_fields(scft_ctx *dst, const scft_ctx *src);
 
 /* Number of kernel launches issued on the context since creation (the
  * benchmark's gpu_launches evidence). */

@@ -408,3 +408,102 @@ def factor_decompose_1024(n: int) -> int:
         if n % d == 0:
             best = d
     return best
+
+
+# --------------------------------------------- convergence and Anderson mixing
+# No reference counterpart (the reference runs a fixed MaxIT with phi_w,
+# cuda_scft.cu:167-253).  Residual = phi_w's direction before the wopt step
+# (cuda_aid.cu:398-408).  Anderson mixing: Anderson (1965) as used for SCFT by
+# Thompson et al. (2004) and Matsen (2009), with an (m+1)-slot ring of (w, d).
+
+def residual(wa, wb, pha, phb, hAB, wcmp=0.10):
+    """(dA, dB, err_max[b], err_rms[b])."""
+    eta = (wa + wb - hAB) / 2
+    psum = 1.0 - pha - phb
+    da = hAB * phb + eta - wa
+    db = hAB * pha + eta - wb
+    da = da - wcmp * psum
+    db = db - wcmp * psum
+    b = wa.shape[0]
+    mx = np.maximum(np.abs(da).reshape(b, -1).max(axis=1), np.abs(db).reshape(b, -1).max(axis=1))
+    rms = np.sqrt(((da * da).reshape(b, -1).sum(axis=1) + (db * db).reshape(b, -1).sum(axis=1))
+                  / (2.0 * da[0].size))
+    return da, db, mx, rms
+
+
+def anderson_weights(G, c, hist, m1, err_max, start, lam, wopt):
+    """Per-instance slot weights a[m1] and step; simple step when err_max >=
+    start or no history (mirrors the device solve, including its 1e-12
+    diagonal shift)."""
+    a = np.zeros(m1)
+    if hist == 0 or not (err_max < start):
+        a[c] = 1.0
+        return a, wopt
+    slot = lambda i: (c - i) % m1
+    n = hist
+    U = np.empty((n, n))
+    V = np.empty(n)
+    gcc = G[c, c]
+    for i in range(n):
+        si = slot(i + 1)
+        V[i] = gcc - G[c, si]
+        for j in range(n):
+            sj = slot(j + 1)
+            U[i, j] = gcc - G[c, si] - G[c, sj] + G[si, sj]
+    dmax = np.abs(np.diag(U)).max()
+    U = U + np.eye(n) * (1e-12 * dmax + 1e-300)
+    x = np.linalg.solve(U, V)
+    for i in range(n):
+        a[slot(i + 1)] = x[i]
+    a[c] = 1.0 - x.sum()
+    return a, lam
+
+
+def converge_loop(wa, wb, p: Params, tol, max_it, mixing="anderson", m=20, lam=0.5,
+                  start=1e-2):
+    """Iterate Free's body (average_value x2, getConc, field update) until
+    max(err_max) < tol; returns (wa, wb, pha, phb, Q, iters, err_history)."""
+    kdz = kxyzdz_half(p)
+    b = wa.shape[0]
+    m1 = m + 1
+    hw = [None] * m1
+    hd = [None] * m1
+    G = np.zeros((b, m1, m1))
+    count = 0
+    errs = []
+    it = 0
+    pha = phb = Q = None
+    while it < max_it:
+        it += 1
+        wa = average_value(wa)
+        wb = average_value(wb)
+        cc = get_conc(wa, wb, p, kdz)
+        wa, pha, phb, Q = cc.wa, cc.pha, cc.phb, cc.Q
+        da, db, emax, erms = residual(wa, wb, pha, phb, p.hAB, p.wcmp)
+        errs.append(emax.max())
+        if mixing == "simple":
+            wa = wa + p.wopt * da
+            wb = wb + p.wopt * db
+        else:
+            c = count % m1
+            hist = min(count, m)
+            hw[c] = np.concatenate([wa.reshape(b, -1), wb.reshape(b, -1)], axis=1)
+            hd[c] = np.concatenate([da.reshape(b, -1), db.reshape(b, -1)], axis=1)
+            for k in range(hist + 1):
+                j = (c - k) % m1
+                g = (hd[c] * hd[j]).sum(axis=1)
+                G[:, c, j] = g
+                G[:, j, c] = g
+            new = np.zeros_like(hw[c])
+            for bi in range(b):
+                a, l = anderson_weights(G[bi], c, hist, m1, emax[bi], start, lam, p.wopt)
+                for j in range(m1):
+                    if a[j] != 0.0:
+                        new[bi] += a[j] * (hw[j][bi] + l * hd[j][bi])
+            M = p.M
+            wa = new[:, :M].reshape(wa.shape)
+            wb = new[:, M:].reshape(wb.shape)
+            count += 1
+        if emax.max() < tol:
+            break
+    return wa, wb, pha, phb, Q, it, errs

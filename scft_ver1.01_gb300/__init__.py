@@ -36,8 +36,10 @@ EXPORTS = [
     "scft_get_Q", "scft_phi_w", "scft_free_energy", "scft_iterate", "scft_free",
     "scft_synchronize", "scft_launch_count", "scft_read_ab_txt", "scft_read_phi_dat",
     "scft_write_pha_dat", "scft_time_iterations", "scft_profile_enable", "scft_profile_read",
-    "scft_split_step_noalloc", "scft_noalloc_last_error",
+    "scft_split_step_noalloc", "scft_noalloc_last_error", "scft_get_residual", "scft_converge",
+    "scft_copy_fields",
 ]
+FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
 
 
 class ScftParams(C.Structure):
@@ -49,7 +51,8 @@ class ScftParams(C.Structure):
         ("batch", C.c_int), ("precision", C.c_int),
         ("wopt", C.c_double), ("wcmp", C.c_double),
         ("mixing", C.c_int), ("anderson_history", C.c_int), ("anderson_lambda", C.c_double),
-        ("device", C.c_int), ("flags", C.c_int), ("reserved", C.c_int * 7),
+        ("device", C.c_int), ("flags", C.c_int), ("anderson_start", C.c_double),
+        ("reserved", C.c_int * 5),
     ]
 
 
@@ -104,6 +107,9 @@ def load_library(path: str | None = None):
         "scft_split_step_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                               C.c_double, C.c_double, C.c_int, vp, vp, vp, vp]),
         "scft_noalloc_last_error": (C.c_char_p, []),
+        "scft_get_residual": (C.c_int, [vp, dp, dp]),
+        "scft_converge": (C.c_int, [vp, C.c_double, C.c_int, C.POINTER(C.c_int), dp]),
+        "scft_copy_fields": (C.c_int, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -260,6 +266,22 @@ class Context:
 
     def launch_count(self) -> int:
         return int(self.lib.scft_launch_count(self.h))
+
+    def residual(self):
+        """-> (err_max[batch], err_rms[batch]) of the last field update."""
+        mx, rms = np.empty(self.shape[0]), np.empty(self.shape[0])
+        self._ck(self.lib.scft_get_residual(self.h, _dptr(mx), _dptr(rms)))
+        return mx, rms
+
+    def converge(self, tol: float, max_it: int):
+        """Iterate to max-norm residual < tol -> (iterations, free energy [batch, 5])."""
+        it = C.c_int()
+        out = np.empty((self.shape[0], 5))
+        self._ck(self.lib.scft_converge(self.h, tol, max_it, C.byref(it), _dptr(out)))
+        return it.value, out
+
+    def copy_fields_from(self, other: "Context"):
+        self._ck(self.lib.scft_copy_fields(self.h, other.h))
 
     def time_iterations(self, n: int) -> float:
         """Device milliseconds of n SCF iterations (events on the library's stream)."""

@@ -2,6 +2,7 @@
 // propagator march, getConc, mixing, free energy and the SCF loop.  Host
 // code only; kernels live in k_line.cu / k_fields.cu.
 #include <math.h>
+#include <cmath>
 #include <stdio.h>
 #include <string.h>
 
@@ -357,9 +358,43 @@ int get_conc(scft_ctx *ctx) {
   return ctx->rbytes == 4 ? q_and_phi<float>(ctx) : q_and_phi<double>(ctx);
 }
 
+// The field update.  Simple mixing is phi_w (cuda_aid.cu:382-416) with its
+// residual reduced on the way; Anderson mixing stores (w, d) in the ring,
+// extends the FP64 Gram matrix by one row, solves the small least-squares
+// problem on the device and applies the mixed step.  No host round trip.
 int mix(scft_ctx *ctx) {
-  CKL(scft::launch_phi_w(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->p.wopt,
-                         ctx->p.wcmp, ctx->M, ctx->batch, ctx->st));
+  const long long M = ctx->M;
+  const int B = ctx->batch;
+  if (ctx->p.mixing == SCFT_MIX_SIMPLE) {
+    CKL(scft::launch_residual(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->p.wcmp,
+                              ctx->p.wopt, M, B, nullptr, nullptr, ctx->rpartial, ctx->nblk,
+                              ctx->res, ctx->st));
+    ctx->launches += 1;
+    return SCFT_OK;
+  }
+  const int m = ctx->p.anderson_history, m1 = ctx->m1;
+  const int c = (int)(ctx->and_count % m1);
+  const int hist = (int)(ctx->and_count < m ? ctx->and_count : m);
+  CKL(scft::launch_residual(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->p.wcmp, 0.0,
+                            M, B, ctx->hist_w[c], ctx->hist_d[c], ctx->rpartial, ctx->nblk,
+                            ctx->res, ctx->st));
+  const double *dj[33], *wj[33];
+  int slots[33];
+  for (int k = 0; k <= hist; ++k) {
+    const int j = ((c - k) % m1 + m1) % m1;
+    slots[k] = j;
+    dj[k] = ctx->hist_d[j];
+    wj[k] = ctx->hist_w[j];
+  }
+  CKL(scft::launch_gram_row(ctx->hist_d[c], dj, slots, hist + 1, c, m1, M, B, ctx->rpartial,
+                            ctx->nblk, ctx->gram, ctx->st));
+  CKL(scft::launch_anderson_solve(ctx->gram, ctx->res, c, hist, m1, ctx->p.anderson_start,
+                                  ctx->p.anderson_lambda, ctx->p.wopt, B, ctx->and_a,
+                                  ctx->and_lam, ctx->st));
+  CKL(scft::launch_anderson_update(ctx->wa, ctx->wb, wj, dj, slots, hist + 1, ctx->and_a,
+                                   ctx->and_lam, m1, M, B, ctx->st));
+  ctx->launches += 2;
+  ctx->and_count++;
   return SCFT_OK;
 }
 
@@ -416,6 +451,12 @@ void free_all(scft_ctx *ctx) {
   if (ctx->st2) cudaStreamDestroy(ctx->st2);
   cudaFree(ctx->partial); cudaFree(ctx->sum); cudaFree(ctx->Q); cudaFree(ctx->ffl);
   cudaFree(ctx->fe5); cudaFree(ctx->tables); cudaFree(ctx->dev_err);
+  cudaFree(ctx->res); cudaFree(ctx->rpartial); cudaFree(ctx->gram); cudaFree(ctx->and_a);
+  cudaFree(ctx->and_lam);
+  for (double *h : ctx->hist_w) cudaFree(h);
+  for (double *h : ctx->hist_d) cudaFree(h);
+  ctx->hist_w.clear();
+  ctx->hist_d.clear();
   for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
   ctx->prof_events.clear();
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -445,7 +486,8 @@ int scft_params_default(scft_params *p) {
   p->wcmp = 0.10;
   p->mixing = SCFT_MIX_SIMPLE;
   p->anderson_history = 20;
-  p->anderson_lambda = 0.1;
+  p->anderson_lambda = 0.5;
+  p->anderson_start = 0.1;
   p->device = 0;
   return SCFT_OK;
 }
@@ -486,8 +528,12 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
   if (p.precision != SCFT_PREC_FP64 && p.precision != SCFT_PREC_FP32)
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad precision");
-  if (p.mixing != SCFT_MIX_SIMPLE)
-    return scft_fail(nullptr, SCFT_ERR_UNSUPPORTED, "only simple mixing is available");
+  if (p.mixing != SCFT_MIX_SIMPLE && p.mixing != SCFT_MIX_ANDERSON)
+    return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad mixing mode");
+  if (p.mixing == SCFT_MIX_ANDERSON &&
+      (p.anderson_history < 1 || p.anderson_history > 32 || !(p.anderson_lambda > 0)))
+    return scft_fail(nullptr, SCFT_ERR_INVALID_ARG,
+                     "Anderson history must be 1..32 and its step positive");
   if (!scft_grid_supported(p.nx, p.ny, p.nz))
     return scft_fail(nullptr, SCFT_ERR_UNSUPPORTED,
                      "grid unsupported: Nx must be even, Ny/Nz even or 1, each <= 4096 with "
@@ -547,7 +593,19 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   ok = ok && alloc((void **)&ctx->partial, 8 * B * 3 * ctx->nblk) &&
        alloc((void **)&ctx->sum, 8 * B) && alloc((void **)&ctx->Q, 8 * B) &&
        alloc((void **)&ctx->ffl, 8 * B) && alloc((void **)&ctx->fe5, 8 * 5 * B) &&
-       alloc((void **)&ctx->dev_err, sizeof(unsigned));
+       alloc((void **)&ctx->dev_err, sizeof(unsigned)) &&
+       alloc((void **)&ctx->res, 8 * 2 * B) &&
+       alloc((void **)&ctx->rpartial, 8 * B * scft::anderson_max_slots() * ctx->nblk);
+  if (ok && p.mixing == SCFT_MIX_ANDERSON) {
+    ctx->m1 = p.anderson_history + 1;
+    ctx->hist_w.assign(ctx->m1, nullptr);
+    ctx->hist_d.assign(ctx->m1, nullptr);
+    for (int j = 0; ok && j < ctx->m1; ++j)
+      ok = alloc((void **)&ctx->hist_w[j], 8 * 2 * M * B) &&
+           alloc((void **)&ctx->hist_d[j], 8 * 2 * M * B);
+    ok = ok && alloc((void **)&ctx->gram, 8 * B * ctx->m1 * ctx->m1) &&
+         alloc((void **)&ctx->and_a, 8 * B * ctx->m1) && alloc((void **)&ctx->and_lam, 8 * B);
+  }
   if (!ok) {
     cudaGetLastError();
     return fail(SCFT_ERR_NO_MEMORY, "device allocation failed");
@@ -661,6 +719,7 @@ int scft_set_field(scft_ctx *ctx, int field, const double *src) {
   if (!d || !src) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad field or null pointer");
   CK(cudaMemcpyAsync(d, src, sizeof(double) * ctx->M * ctx->batch, cudaMemcpyHostToDevice, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
+  if (field == SCFT_FIELD_WA || field == SCFT_FIELD_WB) ctx->and_count = 0;  // new fields, new history
   return SCFT_OK;
 }
 
@@ -782,6 +841,62 @@ int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir) {
 int scft_synchronize(scft_ctx *ctx) {
   if (!ctx) return SCFT_ERR_INVALID_ARG;
   return sync_check(ctx);
+}
+
+int scft_get_residual(scft_ctx *ctx, double *err_max, double *err_rms) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  std::vector<double> e(2 * ctx->batch);
+  CK(cudaMemcpyAsync(e.data(), ctx->res, sizeof(double) * e.size(), cudaMemcpyDeviceToHost,
+                     ctx->st));
+  if (int rc = sync_check(ctx)) return rc;
+  for (int b = 0; b < ctx->batch; ++b) {
+    if (err_max) err_max[b] = e[2 * b];
+    if (err_rms) err_rms[b] = e[2 * b + 1];
+  }
+  return SCFT_OK;
+}
+
+int scft_converge(scft_ctx *ctx, double tol, int max_it, int *iters, double *out5) {
+  if (!ctx || max_it < 0 || !(tol > 0)) return SCFT_ERR_INVALID_ARG;
+  std::vector<double> e(ctx->batch);
+  int it = 0;
+  while (it < max_it) {
+    int rc = iterate_once(ctx);
+    if (rc) return rc;
+    ++it;
+    if ((rc = scft_get_residual(ctx, e.data(), nullptr))) return rc;
+    bool done = true;
+    for (double v : e) {
+      if (!std::isfinite(v)) {
+        if (iters) *iters = it;
+        return scft_fail(ctx, SCFT_ERR_NOT_FINITE, "residual is not finite (diverged)");
+      }
+      if (!(v < tol)) done = false;
+    }
+    if (done) break;
+  }
+  if (iters) *iters = it;
+  if (out5) {
+    int rc = free_energy_dev(ctx);
+    if (rc) return rc;
+    return read_fe(ctx, out5);
+  }
+  return SCFT_OK;
+}
+
+int scft_copy_fields(scft_ctx *dst, const scft_ctx *src) {
+  if (!dst || !src) return SCFT_ERR_INVALID_ARG;
+  scft_ctx *ctx = dst;   // errors are reported on the destination
+  if (dst->M != src->M || dst->batch != src->batch)
+    return scft_fail(dst, SCFT_ERR_INVALID_ARG, "contexts differ in grid or batch");
+  const size_t bytes = sizeof(double) * dst->M * dst->batch;
+  CK(cudaStreamSynchronize(src->st));
+  CK(cudaMemcpyAsync(dst->wa, src->wa, bytes, cudaMemcpyDeviceToDevice, dst->st));
+  CK(cudaMemcpyAsync(dst->wb, src->wb, bytes, cudaMemcpyDeviceToDevice, dst->st));
+  CK(cudaMemcpyAsync(dst->pha, src->pha, bytes, cudaMemcpyDeviceToDevice, dst->st));
+  CK(cudaMemcpyAsync(dst->phb, src->phb, bytes, cudaMemcpyDeviceToDevice, dst->st));
+  dst->and_count = 0;   // the Anderson history belongs to the old fields
+  return sync_check(dst);
 }
 
 long long scft_launch_count(const scft_ctx *ctx) { return ctx ? ctx->launches : -1; }

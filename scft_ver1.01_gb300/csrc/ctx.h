@@ -40,6 +40,15 @@ struct scft_ctx {
   int nblk = 1;
   double *partial = nullptr;    // [batch][3][nblk]
   double *sum = nullptr, *Q = nullptr, *ffl = nullptr, *fe5 = nullptr;
+  // residual and Anderson mixing
+  double *res = nullptr;          // [batch][2]: residual max|d|, rms(d)
+  double *rpartial = nullptr;     // [batch][33][nblk] reduction partials
+  int m1 = 0;                     // Anderson ring slots (history + 1)
+  std::vector<double *> hist_w, hist_d;   // ring of [batch][2][M]
+  double *gram = nullptr;         // [batch][m1][m1]
+  double *and_a = nullptr;        // [batch][m1] slot weights
+  double *and_lam = nullptr;      // [batch] step
+  long long and_count = 0;        // iterations stored in the ring
   // spectral tables (twiddles + gains of each pass), device
   void *tables = nullptr;
   std::vector<scft::AxisPlan> passes;

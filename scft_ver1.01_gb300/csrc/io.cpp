@@ -51,6 +51,7 @@ int scft_read_phi_dat(scft_ctx *ctx, const char *path, int inst) {
   }
   fclose(fp);
   double *dst[4] = {ctx->pha, ctx->phb, ctx->wa, ctx->wb};
+  ctx->and_count = 0;   // new fields: the Anderson history restarts
   std::vector<double> *src[4] = {&a, &b, &c, &d};
   cudaSetDevice(ctx->p.device);
   for (int k = 0; k < 4; ++k) {

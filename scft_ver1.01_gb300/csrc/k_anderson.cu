@@ -1,0 +1,320 @@
+// Field-update kernels with a convergence measure: simple mixing with its
+// residual, and Anderson mixing (no reference counterpart; the reference has
+// only phi_w, cuda_aid.cu:382-416).
+//
+// Residual (phi_w's update direction before the wopt step, cuda_aid.cu:398-408):
+//   dA = hAB*phB + eta - wA - wcmp*(1-phA-phB),  dB = hAB*phA + eta - wB - wcmp*(...)
+// Anderson (Anderson 1965, in the form used for SCFT by Thompson et al. 2004 and
+// Matsen 2009): keep the last m+1 pairs (w_j, d_j) in a ring; with G_ij = <d_i, d_j>
+// (both fields, all points, FP64) and the current slot c,
+//   U_ij = G_cc - G_c,ci - G_c,cj + G_ci,cj ,  V_i = G_cc - G_c,ci   (ci = slot c-i)
+//   solve U x = V (FP64, one warp);  a_c = 1 - sum x_i, a_ci = x_i
+//   w_new = sum_j a_j (w_j + lambda d_j)
+// An instance whose max|d| is still above `start` (or with no history yet)
+// takes the simple step w_new = w_c + wopt d_c, decided on the device.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace scft {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double blk_sum(double v, double *sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  return r;
+}
+__device__ __forceinline__ double blk_max(double v, double *sh) {
+  v = warp_max(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    r = warp_max(r);
+  }
+  return r;
+}
+
+// Residual of instance blockIdx.y; optionally copies w and d into a history
+// slot ([b][2][M] layout) and applies the simple step in place (wopt != 0).
+// partial[(b*2 + {0: max|d|, 1: sum d^2})*nblk + blk]
+__global__ void k_residual(double *__restrict__ wa, double *__restrict__ wb,
+                           const double *__restrict__ pha, const double *__restrict__ phb,
+                           double hAB, double wcmp, double wopt, long long M,
+                           double *__restrict__ hw, double *__restrict__ hd,
+                           double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const long long b = blockIdx.y, o = b * M;
+  double mx = 0.0, ss = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double a = wa[o + i], c = wb[o + i], pa = pha[o + i], pb = phb[o + i];
+    const double eta = (a + c - hAB) / 2;
+    const double psum = 1.0 - pa - pb;
+    double da = hAB * pb + eta - a;
+    double db = hAB * pa + eta - c;
+    da -= wcmp * psum;
+    db -= wcmp * psum;
+    mx = fmax(mx, fmax(fabs(da), fabs(db)));
+    ss += da * da + db * db;
+    if (hw) {
+      hw[(2 * b) * M + i] = a;
+      hw[(2 * b + 1) * M + i] = c;
+      hd[(2 * b) * M + i] = da;
+      hd[(2 * b + 1) * M + i] = db;
+    }
+    if (wopt != 0.0) {
+      wa[o + i] = a + wopt * da;
+      wb[o + i] = c + wopt * db;
+    }
+  }
+  const double rm = blk_max(mx, sh);
+  const double rs = blk_sum(ss, sh);
+  if (threadIdx.x == 0) {
+    partial[(b * 2 + 0) * gridDim.x + blockIdx.x] = rm;
+    partial[(b * 2 + 1) * gridDim.x + blockIdx.x] = rs;
+  }
+}
+
+// err[b*2 + 0] = max|d|, err[b*2 + 1] = rms
+__global__ void k_residual_finalize(const double *__restrict__ partial, int nblk, long long M,
+                                    double *__restrict__ err) {
+  __shared__ double sh[32];
+  const int b = blockIdx.x;
+  double mx = 0.0, ss = 0.0;
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
+    mx = fmax(mx, partial[(b * 2 + 0) * nblk + i]);
+    ss += partial[(b * 2 + 1) * nblk + i];
+  }
+  mx = blk_max(mx, sh);
+  ss = blk_sum(ss, sh);
+  if (threadIdx.x == 0) {
+    err[b * 2 + 0] = mx;
+    err[b * 2 + 1] = sqrt(ss / (2.0 * (double)M));
+  }
+}
+
+// Gram row of slot c: <d_c, d_j> for the listed slots j (nj <= kMaxSlots).
+// partial[(b*kMaxSlots + k)*nblk + blk]
+constexpr int kMaxSlots = 33;
+struct SlotList {
+  const double *d[kMaxSlots];
+  int slot[kMaxSlots];
+  int n;
+};
+__global__ void k_gram_row(const double *__restrict__ dc, SlotList sl, long long M,
+                           double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const long long b = blockIdx.y;
+  double acc[kMaxSlots];
+#pragma unroll
+  for (int k = 0; k < kMaxSlots; ++k) acc[k] = 0.0;
+  const long long n2 = 2 * M;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double x = dc[b * n2 + i];
+#pragma unroll
+    for (int k = 0; k < kMaxSlots; ++k)
+      if (k < sl.n) acc[k] += x * sl.d[k][b * n2 + i];
+  }
+#pragma unroll 1
+  for (int k = 0; k < sl.n; ++k) {
+    const double r = blk_sum(acc[k], sh);
+    if (threadIdx.x == 0) partial[(b * kMaxSlots + k) * gridDim.x + blockIdx.x] = r;
+  }
+}
+
+// Finalise the Gram row into the ring matrix G[b][(m+1)x(m+1)] (symmetric).
+__global__ void k_gram_finalize(const double *__restrict__ partial, int nblk, SlotList sl, int c,
+                                int m1, double *__restrict__ G) {
+  __shared__ double sh[32];
+  const int b = blockIdx.y, k = blockIdx.x;
+  if (k >= sl.n) return;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x)
+    s += partial[((long long)b * kMaxSlots + k) * nblk + i];
+  s = blk_sum(s, sh);
+  if (threadIdx.x == 0) {
+    const int j = sl.slot[k];
+    G[((long long)b * m1 + c) * m1 + j] = s;
+    G[((long long)b * m1 + j) * m1 + c] = s;
+  }
+}
+
+// One warp per instance: weights a[b][slot] and the step lam_eff[b].
+// hist = number of previous slots (newest first: c-1, c-2, ...).
+__global__ void k_anderson_solve(const double *__restrict__ G, const double *__restrict__ err,
+                                 int c, int hist, int m1, double start, double lambda,
+                                 double wopt, double *__restrict__ a, double *__restrict__ lam) {
+  __shared__ double U[32][33];
+  __shared__ double V[32];
+  const int b = blockIdx.x, lane = threadIdx.x;
+  const double *Gb = G + (long long)b * m1 * m1;
+  double *ab = a + (long long)b * m1;
+  for (int j = lane; j < m1; j += 32) ab[j] = 0.0;
+  __syncwarp();
+  const bool simple = hist == 0 || !(err[b * 2] < start);
+  if (simple) {
+    if (lane == 0) {
+      ab[c] = 1.0;
+      lam[b] = wopt;
+    }
+    return;
+  }
+  const int n = hist;
+  auto slot = [&](int i) { return ((c - i) % m1 + m1) % m1; };   // i = 1..n
+  const double gcc = Gb[c * m1 + c];
+  for (int i = 0; i < n; ++i) {
+    if (lane < n) {
+      const int si = slot(i + 1), sj = slot(lane + 1);
+      U[i][lane] = gcc - Gb[c * m1 + si] - Gb[c * m1 + sj] + Gb[si * m1 + sj];
+    }
+  }
+  if (lane < n) V[lane] = gcc - Gb[c * m1 + slot(lane + 1)];
+  __syncwarp();
+  // Tikhonov shift relative to the largest diagonal entry keeps U invertible
+  // when two histories are nearly parallel.
+  double dmax = 0.0;
+  for (int i = 0; i < n; ++i) dmax = fmax(dmax, fabs(U[i][i]));
+  if (lane < n) U[lane][lane] += 1e-12 * dmax + 1e-300;
+  __syncwarp();
+  // Gaussian elimination with partial pivoting; lane r owns row r.
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    if (lane == 0) {
+      double best = fabs(U[k][k]);
+      for (int r = k + 1; r < n; ++r)
+        if (fabs(U[r][k]) > best) { best = fabs(U[r][k]); piv = r; }
+    }
+    piv = __shfl_sync(0xffffffffu, piv, 0);
+    if (piv != k) {
+      if (lane <= n) {
+        if (lane < n) {
+          const double t = U[k][lane]; U[k][lane] = U[piv][lane]; U[piv][lane] = t;
+        }
+      }
+      if (lane == 0) { const double t = V[k]; V[k] = V[piv]; V[piv] = t; }
+    }
+    __syncwarp();
+    const double pk = U[k][k];
+    if (lane > k && lane < n) {
+      const double f = U[lane][k] / pk;
+      for (int j = k; j < n; ++j) U[lane][j] -= f * U[k][j];
+      V[lane] -= f * V[k];
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    double x[32];
+    double sx = 0.0;
+    for (int i = n - 1; i >= 0; --i) {
+      double s = V[i];
+      for (int j = i + 1; j < n; ++j) s -= U[i][j] * x[j];
+      x[i] = s / U[i][i];
+    }
+    for (int i = 0; i < n; ++i) {
+      ab[slot(i + 1)] = x[i];
+      sx += x[i];
+    }
+    ab[c] = 1.0 - sx;
+    lam[b] = lambda;
+  }
+}
+
+// w_new = sum_j a_j (w_j + lam d_j) over the listed slots.
+struct SlotPairs {
+  const double *w[kMaxSlots];
+  const double *d[kMaxSlots];
+  int idx[kMaxSlots];
+  int n;
+};
+__global__ void k_anderson_update(double *__restrict__ wa, double *__restrict__ wb,
+                                  SlotPairs sp, const double *__restrict__ a,
+                                  const double *__restrict__ lam, int m1, long long M) {
+  const long long b = blockIdx.y;
+  const double l = lam[b];
+  const long long n2 = 2 * M;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2;
+       i += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+#pragma unroll 4
+    for (int k = 0; k < sp.n; ++k) {
+      const double aj = a[b * m1 + sp.idx[k]];
+      if (aj != 0.0) s += aj * (sp.w[k][b * n2 + i] + l * sp.d[k][b * n2 + i]);
+    }
+    if (i < M) wa[b * M + i] = s;
+    else wb[b * M + (i - M)] = s;
+  }
+}
+
+inline int grid_for(long long n) {
+  long long g = (n + kThreads - 1) / kThreads;
+  if (g > 152 * 8) g = 152 * 8;
+  return g < 1 ? 1 : (int)g;
+}
+
+}  // namespace
+
+int anderson_max_slots() { return kMaxSlots; }
+
+cudaError_t launch_residual(double *wa, double *wb, const double *pha, const double *phb,
+                            double hAB, double wcmp, double wopt, long long M, int batch,
+                            double *hw, double *hd, double *partial, int nblk, double *err,
+                            cudaStream_t st) {
+  k_residual<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, wcmp, wopt, M, hw,
+                                                    hd, partial);
+  k_residual_finalize<<<batch, kThreads, 0, st>>>(partial, nblk, M, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gram_row(const double *dc, const double *const *dj, const int *slots, int n,
+                            int c, int m1, long long M, int batch, double *partial, int nblk,
+                            double *G, cudaStream_t st) {
+  SlotList sl;
+  sl.n = n;
+  for (int k = 0; k < n; ++k) {
+    sl.d[k] = dj[k];
+    sl.slot[k] = slots[k];
+  }
+  k_gram_row<<<dim3(nblk, batch), kThreads, 0, st>>>(dc, sl, M, partial);
+  k_gram_finalize<<<dim3(n, batch), kThreads, 0, st>>>(partial, nblk, sl, c, m1, G);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_anderson_solve(const double *G, const double *err, int c, int hist, int m1,
+                                  double start, double lambda, double wopt, int batch,
+                                  double *a, double *lam, cudaStream_t st) {
+  k_anderson_solve<<<batch, 32, 0, st>>>(G, err, c, hist, m1, start, lambda, wopt, a, lam);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_anderson_update(double *wa, double *wb, const double *const *hw,
+                                   const double *const *hd, const int *idx, int n,
+                                   const double *a, const double *lam, int m1, long long M,
+                                   int batch, cudaStream_t st) {
+  SlotPairs sp;
+  sp.n = n;
+  for (int k = 0; k < n; ++k) {
+    sp.w[k] = hw[k];
+    sp.d[k] = hd[k];
+    sp.idx[k] = idx[k];
+  }
+  k_anderson_update<<<dim3(grid_for(2 * M), batch), kThreads, 0, st>>>(wa, wb, sp, a, lam, m1,
+                                                                       M);
+  return cudaGetLastError();
+}
+
+}  // namespace scft

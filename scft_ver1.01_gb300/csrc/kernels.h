@@ -65,6 +65,26 @@ size_t line_filter_smem_bytes(const AxisPlan &ap, size_t real_bytes);
 constexpr int kLineSmemMax = 200 * 1024;
 cudaError_t line_filter_prepare();
 
+// ---- residual and Anderson mixing (k_anderson.cu) ----
+int anderson_max_slots();
+// residual of phi_w's update (err[b][2] = max, rms); optionally stores w, d
+// into a history slot and/or applies the simple step w += wopt*d (2 kernels)
+cudaError_t launch_residual(double *wa, double *wb, const double *pha, const double *phb,
+                            double hAB, double wcmp, double wopt, long long M, int batch,
+                            double *hw, double *hd, double *partial, int nblk, double *err,
+                            cudaStream_t st);
+// Gram row <d_c, d_j> into the ring matrix (2 kernels)
+cudaError_t launch_gram_row(const double *dc, const double *const *dj, const int *slots, int n,
+                            int c, int m1, long long M, int batch, double *partial, int nblk,
+                            double *G, cudaStream_t st);
+cudaError_t launch_anderson_solve(const double *G, const double *err, int c, int hist, int m1,
+                                  double start, double lambda, double wopt, int batch,
+                                  double *a, double *lam, cudaStream_t st);
+cudaError_t launch_anderson_update(double *wa, double *wb, const double *const *hw,
+                                   const double *const *hd, const int *idx, int n,
+                                   const double *a, const double *lam, int m1, long long M,
+                                   int batch, cudaStream_t st);
+
 // ---- field kernels (k_fields.cu) ----
 // W = exp(-w*ds2) in precision R, for batch*M points (w is FP64).
 template <typename R>

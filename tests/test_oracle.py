@@ -167,3 +167,20 @@ def test_parse_ab_txt(orc):
     p = orc.parse_ab_txt(text)
     assert (p.nx, p.ny, p.nz, p.batch, p.intag) == (64, 64, 64, 2, 1024)
     assert (p.hAB, p.fA, p.ds0, p.lz) == (18.0, 0.36, 0.005, 3.8)
+
+
+def test_oracle_anderson_beats_simple_mixing(orc):
+    # the same lamellar start: Anderson reaches 1e-4 quickly, simple mixing does not
+    p = P(orc, nx=16, ny=4, nz=4, lx=4.0, hAB=15.0, fA=0.5, ds0=0.02)
+    x = np.arange(p.nx) * p.lx / p.nx
+    base = 1.5 * np.cos(2 * np.pi * x / p.lx) * np.ones(p.shape)
+    rng = np.random.default_rng(0)
+    wa = base[None] + rng.normal(0, 0.01, (1,) + p.shape)
+    wb = -base[None] + rng.normal(0, 0.01, (1,) + p.shape)
+    ra = orc.converge_loop(wa, wb, p, 1e-4, 300, mixing="anderson", m=10, lam=0.5, start=0.1)
+    rs = orc.converge_loop(wa, wb, p, 1e-4, 300, mixing="simple")
+    assert ra[6][-1] < 1e-4
+    assert ra[5] < rs[5] or rs[6][-1] > 1e-4
+    # at the saddle point incompressibility holds and the residual vanishes
+    _, _, emax, _ = orc.residual(ra[0], ra[1], ra[2], ra[3], p.hAB, p.wcmp)
+    assert emax[0] < 1e-3
