@@ -519,7 +519,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   if (!pin || !out) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "null argument");
   *out = nullptr;
   const scft_params &p = *pin;
-  for (int i = 0; i < 7; ++i)
+  for (size_t i = 0; i < sizeof(p.reserved) / sizeof(p.reserved[0]); ++i)
     if (p.reserved[i]) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "reserved fields must be 0");
   if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_PIPE | SCFT_FLAG_TWO_STREAMS |
                   SCFT_FLAG_LOCKSTEP | SCFT_FLAG_NO_XY))

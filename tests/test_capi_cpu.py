@@ -91,6 +91,27 @@ def test_read_ab_txt_errors(pkg, tmp_path):
     assert e.value.status == pkg.ERR_IO
 
 
+def test_params_layout_matches_header(pkg, tmp_path):
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "sz.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "scft_capi.h"\n'
+                   'int main(void){printf("%zu %zu %zu\\n", sizeof(scft_params),'
+                   ' offsetof(scft_params, anderson_start), offsetof(scft_params, flags));'
+                   'return 0;}\n')
+    exe = tmp_path / "sz"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    size, off_start, off_flags = map(int, subprocess.run([str(exe)], capture_output=True,
+                                                          text=True).stdout.split())
+    assert C.sizeof(pkg.ScftParams) == size
+    assert pkg.ScftParams.anderson_start.offset == off_start
+    assert pkg.ScftParams.flags.offset == off_flags
+
+
 def test_library_refuses_to_load_when_missing(pkg, tmp_path):
     with pytest.raises(ImportError):
         pkg.load_library(str(tmp_path / "nope.so"))
