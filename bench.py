@@ -165,6 +165,49 @@ def run_reference(args):
     return 0
 
 
+def converge_leg(pkg, dev, tol=1e-6, max_it=3000):
+    """Seconds to converge (max-norm residual < tol) on the 64^3 double-gyroid
+    config (f=0.36, chiN=18, box 3.8, Ns=200, Anderson history 20): the plain
+    FP64 GPU path against FP32 propagation + FP64 polish.  Wall-clock seconds
+    with a residual check after every iteration, inputs already on the device."""
+    from scft_gb300 import fields as fl
+    n, Lb = 64, 3.8
+    wa, wb = fl.gyroid(n, n, n, Lb, Lb, Lb, 18.0, seed=0)
+    kw = dict(nx=n, ny=n, nz=n, lx=Lb, ly=Lb, lz=Lb, hAB=18.0, fA=0.36, ds0=0.005,
+              mixing=pkg.MIX_ANDERSON, anderson_history=20, anderson_lambda=0.5,
+              anderson_start=0.1, device=dev)
+    out = {"config": "64^3 double gyroid, f=0.36, chiN=18, box 3.8 Rg, Ns=200, Anderson m=20, "
+                     "tol %g (max-norm of the phi_w residual)" % tol}
+    with pkg.Context(precision=pkg.PREC_FP64, **kw) as c64:
+        c64.set_w(wa, wb)
+        c64.iterate(1)                      # plans, graph capture
+        c64.set_w(wa, wb)
+        t0 = time.perf_counter()
+        it64, fe64 = c64.converge(tol, max_it)
+        t64 = time.perf_counter() - t0
+        r64 = float(c64.residual()[0][0])
+    with pkg.Context(precision=pkg.PREC_FP32, **kw) as c32, \
+            pkg.Context(precision=pkg.PREC_FP64, **kw) as pol:
+        c32.set_w(wa, wb)
+        c32.iterate(1)
+        pol.set_w(wa, wb)
+        pol.iterate(1)
+        c32.set_w(wa, wb)
+        t0 = time.perf_counter()
+        it32, _ = c32.converge(1e-4, max_it)     # FP32 residual floor ~1e-5
+        pol.copy_fields_from(c32)
+        itp, fep = pol.converge(tol, max_it)
+        tmx = time.perf_counter() - t0
+        rmx = float(pol.residual()[0][0])
+    out.update(fp64={"seconds": t64, "iterations": it64, "F": fe64[0, 0], "residual": r64},
+               fp32_fp64_polish={"seconds": tmx, "iterations_fp32": it32,
+                                 "iterations_fp64_polish": itp, "F": fep[0, 0],
+                                 "residual": rmx},
+               speedup=t64 / tmx if tmx > 0 else None,
+               F_abs_diff=abs(fep[0, 0] - fe64[0, 0]))
+    return out
+
+
 def run_ours(args):
     import torch
     import __graft_entry__ as ge
@@ -288,6 +331,8 @@ def run_ours(args):
                                             "to the end of the timed region",
                            warmup_iterations_run=nw),
             "wall_s_timed": wall,
+            "converge": (converge_leg(pkg, dev) if (not args.no_converge and ws == 1)
+                         else None),
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -307,6 +352,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--grid", type=int, default=N, help="grid edge (profiling cases only)")
     ap.add_argument("--ns", type=int, default=200, help="contour steps 1/ds (profiling only)")
+    ap.add_argument("--no-converge", action="store_true",
+                    help="skip the seconds-to-converge leg (FP64 vs FP32+FP64 polish)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
