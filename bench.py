@@ -190,7 +190,7 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
     wa, wb = fl.gyroid(n, n, n, Lb, Lb, Lb, 18.0, seed=0)
     kw = dict(nx=n, ny=n, nz=n, lx=Lb, ly=Lb, lz=Lb, hAB=18.0, fA=0.36, ds0=0.005,
               mixing=pkg.MIX_ANDERSON, anderson_history=20, anderson_lambda=0.5,
-              anderson_start=0.1, device=dev)
+              anderson_start=1.0, device=dev)
     out = {"config": "64^3 double gyroid, f=0.36, chiN=18, box 3.8 Rg, Ns=200, Anderson m=20, "
                      "tol %g (max-norm of the phi_w residual)" % tol}
     with pkg.Context(precision=pkg.PREC_FP64, **kw) as c64:

@@ -417,7 +417,11 @@ def factor_decompose_1024(n: int) -> int:
 # Thompson et al. (2004) and Matsen (2009), with an (m+1)-slot ring of (w, d).
 
 def residual(wa, wb, pha, phb, hAB, wcmp=0.10):
-    """(dA, dB, err_max[b], err_rms[b])."""
+    """(dA, dB, err_max[b], err_rms[b], cA, cB): dA, dB are phi_w's raw
+    directions; cA, cB the same with their per-instance means removed.  The
+    field mean is a gauge freedom that average_value removes every iteration
+    (for f != 1/2 the raw direction carries the constant chiN*(1/2 - f)), so
+    the norms and the Anderson history use the mean-free residual."""
     eta = (wa + wb - hAB) / 2
     psum = 1.0 - pha - phb
     da = hAB * phb + eta - wa
@@ -425,10 +429,12 @@ def residual(wa, wb, pha, phb, hAB, wcmp=0.10):
     da = da - wcmp * psum
     db = db - wcmp * psum
     b = wa.shape[0]
-    mx = np.maximum(np.abs(da).reshape(b, -1).max(axis=1), np.abs(db).reshape(b, -1).max(axis=1))
-    rms = np.sqrt(((da * da).reshape(b, -1).sum(axis=1) + (db * db).reshape(b, -1).sum(axis=1))
+    ca = da - da.reshape(b, -1).mean(axis=1).reshape((b,) + (1,) * (da.ndim - 1))
+    cb = db - db.reshape(b, -1).mean(axis=1).reshape((b,) + (1,) * (db.ndim - 1))
+    mx = np.maximum(np.abs(ca).reshape(b, -1).max(axis=1), np.abs(cb).reshape(b, -1).max(axis=1))
+    rms = np.sqrt(((ca * ca).reshape(b, -1).sum(axis=1) + (cb * cb).reshape(b, -1).sum(axis=1))
                   / (2.0 * da[0].size))
-    return da, db, mx, rms
+    return da, db, mx, rms, ca, cb
 
 
 def anderson_weights(G, c, hist, m1, err_max, start, lam, wopt):
@@ -479,7 +485,7 @@ def converge_loop(wa, wb, p: Params, tol, max_it, mixing="anderson", m=20, lam=0
         wb = average_value(wb)
         cc = get_conc(wa, wb, p, kdz)
         wa, pha, phb, Q = cc.wa, cc.pha, cc.phb, cc.Q
-        da, db, emax, erms = residual(wa, wb, pha, phb, p.hAB, p.wcmp)
+        da, db, emax, erms, ca, cb = residual(wa, wb, pha, phb, p.hAB, p.wcmp)
         errs.append(emax.max())
         if mixing == "simple":
             wa = wa + p.wopt * da
@@ -488,7 +494,7 @@ def converge_loop(wa, wb, p: Params, tol, max_it, mixing="anderson", m=20, lam=0
             c = count % m1
             hist = min(count, m)
             hw[c] = np.concatenate([wa.reshape(b, -1), wb.reshape(b, -1)], axis=1)
-            hd[c] = np.concatenate([da.reshape(b, -1), db.reshape(b, -1)], axis=1)
+            hd[c] = np.concatenate([ca.reshape(b, -1), cb.reshape(b, -1)], axis=1)
             for k in range(hist + 1):
                 j = (c - k) % m1
                 g = (hd[c] * hd[j]).sum(axis=1)

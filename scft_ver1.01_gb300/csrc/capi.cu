@@ -369,7 +369,7 @@ int mix(scft_ctx *ctx) {
     CKL(scft::launch_residual(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->p.wcmp,
                               ctx->p.wopt, M, B, nullptr, nullptr, ctx->rpartial, ctx->nblk,
                               ctx->res, ctx->st));
-    ctx->launches += 1;
+    ctx->launches += 3;   // launch_residual issues four kernels
     return SCFT_OK;
   }
   const int m = ctx->p.anderson_history, m1 = ctx->m1;
@@ -393,7 +393,7 @@ int mix(scft_ctx *ctx) {
                                   ctx->and_lam, ctx->st));
   CKL(scft::launch_anderson_update(ctx->wa, ctx->wb, wj, dj, slots, hist + 1, ctx->and_a,
                                    ctx->and_lam, m1, M, B, ctx->st));
-  ctx->launches += 2;
+  ctx->launches += 4;   // residual: 4 kernels, Gram row: 2
   ctx->and_count++;
   return SCFT_OK;
 }
@@ -487,7 +487,7 @@ int scft_params_default(scft_params *p) {
   p->mixing = SCFT_MIX_SIMPLE;
   p->anderson_history = 20;
   p->anderson_lambda = 0.5;
-  p->anderson_start = 0.1;
+  p->anderson_start = 1.0;
   p->device = 0;
   return SCFT_OK;
 }
@@ -594,7 +594,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
        alloc((void **)&ctx->sum, 8 * B) && alloc((void **)&ctx->Q, 8 * B) &&
        alloc((void **)&ctx->ffl, 8 * B) && alloc((void **)&ctx->fe5, 8 * 5 * B) &&
        alloc((void **)&ctx->dev_err, sizeof(unsigned)) &&
-       alloc((void **)&ctx->res, 8 * 2 * B) &&
+       alloc((void **)&ctx->res, 8 * 4 * B) &&   // [b][2] residual norms + [b][2] means
        alloc((void **)&ctx->rpartial, 8 * B * scft::anderson_max_slots() * ctx->nblk);
   if (ok && p.mixing == SCFT_MIX_ANDERSON) {
     ctx->m1 = p.anderson_history + 1;

@@ -48,36 +48,89 @@ __device__ __forceinline__ double blk_max(double v, double *sh) {
   return r;
 }
 
-// Residual of instance blockIdx.y; optionally copies w and d into a history
-// slot ([b][2][M] layout) and applies the simple step in place (wopt != 0).
+__device__ __forceinline__ void phi_w_dir(double a, double c, double pa, double pb, double hAB,
+                                          double wcmp, double &da, double &db) {
+  const double eta = (a + c - hAB) / 2;
+  const double psum = 1.0 - pa - pb;
+  da = hAB * pb + eta - a;
+  db = hAB * pa + eta - c;
+  da -= wcmp * psum;
+  db -= wcmp * psum;
+}
+
+// Per-instance sums of dA and dB: partial[(b*2 + f)*nblk + blk].
+__global__ void k_residual_sum(const double *__restrict__ wa, const double *__restrict__ wb,
+                               const double *__restrict__ pha, const double *__restrict__ phb,
+                               double hAB, double wcmp, long long M,
+                               double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const long long b = blockIdx.y, o = b * M;
+  double sa = 0.0, sb = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x) {
+    double da, db;
+    phi_w_dir(wa[o + i], wb[o + i], pha[o + i], phb[o + i], hAB, wcmp, da, db);
+    sa += da;
+    sb += db;
+  }
+  const double ra = blk_sum(sa, sh);
+  const double rb = blk_sum(sb, sh);
+  if (threadIdx.x == 0) {
+    partial[(b * 2 + 0) * gridDim.x + blockIdx.x] = ra;
+    partial[(b * 2 + 1) * gridDim.x + blockIdx.x] = rb;
+  }
+}
+
+// dmean[b*2 + f] = mean of dA / dB
+__global__ void k_residual_mean(const double *__restrict__ partial, int nblk, long long M,
+                                double *__restrict__ dmean) {
+  __shared__ double sh[32];
+  const int b = blockIdx.x;
+  double sa = 0.0, sb = 0.0;
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
+    sa += partial[(b * 2 + 0) * nblk + i];
+    sb += partial[(b * 2 + 1) * nblk + i];
+  }
+  sa = blk_sum(sa, sh);
+  sb = blk_sum(sb, sh);
+  if (threadIdx.x == 0) {
+    dmean[b * 2 + 0] = sa / (double)M;
+    dmean[b * 2 + 1] = sb / (double)M;
+  }
+}
+
+// Residual of instance blockIdx.y.  The field mean is a gauge freedom
+// (average_value removes it every iteration), so the residual that measures
+// convergence and enters the Anderson history is d = dir - mean(dir); the
+// simple step applies the raw phi_w direction, exactly as the reference.
+// Optionally copies w and d into a history slot ([b][2][M] layout) and applies
+// the simple step in place (wopt != 0).
 // partial[(b*2 + {0: max|d|, 1: sum d^2})*nblk + blk]
 __global__ void k_residual(double *__restrict__ wa, double *__restrict__ wb,
                            const double *__restrict__ pha, const double *__restrict__ phb,
                            double hAB, double wcmp, double wopt, long long M,
-                           double *__restrict__ hw, double *__restrict__ hd,
-                           double *__restrict__ partial) {
+                           const double *__restrict__ dmean, double *__restrict__ hw,
+                           double *__restrict__ hd, double *__restrict__ partial) {
   __shared__ double sh[32];
   const long long b = blockIdx.y, o = b * M;
+  const double ma = dmean[b * 2 + 0], mb = dmean[b * 2 + 1];
   double mx = 0.0, ss = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
        i += (long long)gridDim.x * blockDim.x) {
-    const double a = wa[o + i], c = wb[o + i], pa = pha[o + i], pb = phb[o + i];
-    const double eta = (a + c - hAB) / 2;
-    const double psum = 1.0 - pa - pb;
-    double da = hAB * pb + eta - a;
-    double db = hAB * pa + eta - c;
-    da -= wcmp * psum;
-    db -= wcmp * psum;
-    mx = fmax(mx, fmax(fabs(da), fabs(db)));
-    ss += da * da + db * db;
+    const double a = wa[o + i], c = wb[o + i];
+    double da, db;
+    phi_w_dir(a, c, pha[o + i], phb[o + i], hAB, wcmp, da, db);   // cuda_aid.cu:398-408
+    const double ca = da - ma, cb = db - mb;
+    mx = fmax(mx, fmax(fabs(ca), fabs(cb)));
+    ss += ca * ca + cb * cb;
     if (hw) {
       hw[(2 * b) * M + i] = a;
       hw[(2 * b + 1) * M + i] = c;
-      hd[(2 * b) * M + i] = da;
-      hd[(2 * b + 1) * M + i] = db;
+      hd[(2 * b) * M + i] = ca;
+      hd[(2 * b + 1) * M + i] = cb;
     }
     if (wopt != 0.0) {
-      wa[o + i] = a + wopt * da;
+      wa[o + i] = a + wopt * da;   // phi_w, cuda_aid.cu:410-412
       wb[o + i] = c + wopt * db;
     }
   }
@@ -274,8 +327,12 @@ cudaError_t launch_residual(double *wa, double *wb, const double *pha, const dou
                             double hAB, double wcmp, double wopt, long long M, int batch,
                             double *hw, double *hd, double *partial, int nblk, double *err,
                             cudaStream_t st) {
-  k_residual<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, wcmp, wopt, M, hw,
-                                                    hd, partial);
+  // err holds [b][2] results; err + 2*batch holds the [b][2] means of dA, dB
+  double *dmean = err + 2 * batch;
+  k_residual_sum<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, wcmp, M, partial);
+  k_residual_mean<<<batch, kThreads, 0, st>>>(partial, nblk, M, dmean);
+  k_residual<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, wcmp, wopt, M, dmean,
+                                                    hw, hd, partial);
   k_residual_finalize<<<batch, kThreads, 0, st>>>(partial, nblk, M, err);
   return cudaGetLastError();
 }

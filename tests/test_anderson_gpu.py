@@ -37,7 +37,7 @@ def test_residual_of_simple_mixing(pkg, orc):
     a = orc.average_value(wa)
     b = orc.average_value(wb)
     c = orc.get_conc(a, b, p)
-    _, _, emax, erms = orc.residual(c.wa, b, c.pha, c.phb, p.hAB, p.wcmp)
+    _, _, emax, erms, _, _ = orc.residual(c.wa, b, c.pha, c.phb, p.hAB, p.wcmp)
     np.testing.assert_allclose(mx, emax, rtol=1e-10)
     np.testing.assert_allclose(rms, erms, rtol=1e-10)
 

@@ -182,5 +182,5 @@ def test_oracle_anderson_beats_simple_mixing(orc):
     assert ra[6][-1] < 1e-4
     assert ra[5] < rs[5] or rs[6][-1] > 1e-4
     # at the saddle point incompressibility holds and the residual vanishes
-    _, _, emax, _ = orc.residual(ra[0], ra[1], ra[2], ra[3], p.hAB, p.wcmp)
+    _, _, emax, _, _, _ = orc.residual(ra[0], ra[1], ra[2], ra[3], p.hAB, p.wcmp)
     assert emax[0] < 1e-3
