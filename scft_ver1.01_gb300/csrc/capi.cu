@@ -895,21 +895,10 @@ int scft_copy_fields(scft_ctx *dst, const scft_ctx *src) {
   CK(cudaMemcpyAsync(dst->wb, src->wb, bytes, cudaMemcpyDeviceToDevice, dst->st));
   CK(cudaMemcpyAsync(dst->pha, src->pha, bytes, cudaMemcpyDeviceToDevice, dst->st));
   CK(cudaMemcpyAsync(dst->phb, src->phb, bytes, cudaMemcpyDeviceToDevice, dst->st));
-  if (dst->m1 > 0 && dst->m1 == src->m1) {
-    // Same Anderson ring: carry the (w, d) history and its Gram matrix over,
-    // so a polish continues the quasi-Newton sequence instead of restarting it.
-    for (int j = 0; j < dst->m1; ++j) {
-      CK(cudaMemcpyAsync(dst->hist_w[j], src->hist_w[j], 2 * bytes, cudaMemcpyDeviceToDevice,
-                         dst->st));
-      CK(cudaMemcpyAsync(dst->hist_d[j], src->hist_d[j], 2 * bytes, cudaMemcpyDeviceToDevice,
-                         dst->st));
-    }
-    CK(cudaMemcpyAsync(dst->gram, src->gram, sizeof(double) * dst->batch * dst->m1 * dst->m1,
-                       cudaMemcpyDeviceToDevice, dst->st));
-    dst->and_count = src->and_count;
-  } else {
-    dst->and_count = 0;   // no compatible history: restart Anderson
-  }
+  // Anderson restarts on the copied fields: a history whose residuals came
+  // from FP32 propagation slows an FP64 polish down (measured: 185 polish
+  // iterations with the carried history against 76 with a fresh one).
+  dst->and_count = 0;
   return sync_check(dst);
 }
 
