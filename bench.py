@@ -209,7 +209,9 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
         pol.iterate(1)
         c32.set_w(wa, wb)
         t0 = time.perf_counter()
-        it32, _, _ = converge_timed(c32, 1e-4, max_it, budget_s)   # FP32 floor ~1e-5
+        # FP32 propagation floors the residual near 2e-5; switch to the FP64
+        # polish at 3e-5 (measured: 48 polish iterations, against 76 from 1e-4)
+        it32, _, _ = converge_timed(c32, 3e-5, max_it, budget_s)
         pol.copy_fields_from(c32)
         itp, fep, okp = converge_timed(pol, tol, max_it, budget_s)
         tmx = time.perf_counter() - t0
