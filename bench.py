@@ -226,6 +226,46 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
     return out
 
 
+def batch_sweep_leg(pkg, dev, n_inst=64, iters=3, seed=4):
+    """Config-4 phase-diagram sweep: 64 independent instances, grids drawn from
+    {32^3, 48^3, 64^3}, chiN~U[12,30], f~U[0.25,0.5], box~U[3,5] Rg,
+    Ns~U{100..200}, seeded random fields, FP32 propagation.  Aggregate
+    Gpt*step/s of one group (one graph launch per iteration) against the same
+    instances iterated one after another."""
+    from scft_gb300 import fields as fl
+    rng = np.random.default_rng(seed)
+    ctxs, pts = [], 0
+    for i in range(n_inst):
+        n = int(rng.choice([32, 48, 64]))
+        chin = float(rng.uniform(12, 30))
+        f = float(rng.uniform(0.25, 0.5))
+        box = float(rng.uniform(3.0, 5.0))
+        ns = int(rng.integers(100, 201))
+        c = pkg.Context(nx=n, ny=n, nz=n, lx=box, ly=box, lz=box, hAB=chin, fA=f, ds0=1.0 / ns,
+                        precision=pkg.PREC_FP32, device=dev)
+        wa, wb = fl.random_fields(n, n, n, seed=1000 + i, scale=0.1 * chin)
+        c.set_w(wa, wb)
+        c.iterate(1)                      # capture the member's own march graph
+        pts += 2 * (c.NsA + c.dNsB) * n ** 3
+        ctxs.append(c)
+    seq_ms = 0.0
+    for c in ctxs:
+        c.synchronize()
+        seq_ms += c.time_iterations(iters)
+    with pkg.Group(ctxs) as g:
+        g.iterate(1)
+        grp_ms = g.time_iterations(iters)
+        launches = g.launch_count()
+    for c in ctxs:
+        c.close()
+    seq = pts * iters / (seq_ms / 1e3) / 1e9
+    grp = pts * iters / (grp_ms / 1e3) / 1e9
+    return {"config": "%d instances, grids {32,48,64}^3, chiN U[12,30], f U[0.25,0.5], box "
+                      "U[3,5], Ns U{100..200}, FP32, seed %d" % (n_inst, seed),
+            "sequential_gpt_step_per_s": seq, "group_gpt_step_per_s": grp,
+            "speedup": grp / seq, "iterations": iters, "group_graph_launches": launches}
+
+
 def run_ours(args):
     import torch
     import __graft_entry__ as ge
@@ -351,6 +391,8 @@ def run_ours(args):
             "wall_s_timed": wall,
             "converge": (converge_leg(pkg, dev) if (not args.no_converge and ws == 1)
                          else None),
+            "batch_sweep": (batch_sweep_leg(pkg, dev) if (not args.no_sweep and ws == 1)
+                            else None),
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -370,6 +412,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--grid", type=int, default=N, help="grid edge (profiling cases only)")
     ap.add_argument("--ns", type=int, default=200, help="contour steps 1/ds (profiling only)")
+    ap.add_argument("--no-sweep", action="store_true",
+                    help="skip the 64-instance heterogeneous sweep leg")
     ap.add_argument("--no-converge", action="store_true",
                     help="skip the seconds-to-converge leg (FP64 vs FP32+FP64 polish)")
     args = ap.parse_args()

@@ -204,6 +204,21 @@ int scft_profile_enable(scft_ctx *ctx, int enable);
 int scft_profile_read(scft_ctx *ctx, double *march_ms, long long *n_marches,
                       double *point_steps);
 
+/* ---- heterogeneous batched sweeps (no reference counterpart: the
+ * reference's batch shares one grid and parameter set, init.cpp:86-94) ----
+ * A group advances many contexts -- any mix of grids, xN, f, boxes, ds0 -- on
+ * one device.  Each group iteration is one CUDA-graph launch that runs every
+ * member's average_value x2 + getConc concurrently on the members' streams,
+ * followed by each member's field update.  Members stay usable on their own;
+ * do not use a member concurrently with its group. */
+typedef struct scft_group scft_group;
+int scft_group_create(scft_ctx *const *ctxs, int n, scft_group **out);
+void scft_group_destroy(scft_group *g);
+const char *scft_group_last_error(const scft_group *g);
+int scft_group_iterate(scft_group *g, int n_iter);
+int scft_group_time_iterations(scft_group *g, int n_iter, double *ms);
+long long scft_group_launch_count(const scft_group *g);
+
 /* ---- split step without device allocation ----
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * where they advance a propagator: a framework that owns all device memory

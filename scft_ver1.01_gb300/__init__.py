@@ -37,7 +37,8 @@ EXPORTS = [
     "scft_synchronize", "scft_launch_count", "scft_read_ab_txt", "scft_read_phi_dat",
     "scft_write_pha_dat", "scft_time_iterations", "scft_profile_enable", "scft_profile_read",
     "scft_split_step_noalloc", "scft_noalloc_last_error", "scft_get_residual", "scft_converge",
-    "scft_copy_fields",
+    "scft_copy_fields", "scft_group_create", "scft_group_destroy", "scft_group_last_error",
+    "scft_group_iterate", "scft_group_time_iterations", "scft_group_launch_count",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
 
@@ -110,6 +111,12 @@ def load_library(path: str | None = None):
         "scft_get_residual": (C.c_int, [vp, dp, dp]),
         "scft_converge": (C.c_int, [vp, C.c_double, C.c_int, C.POINTER(C.c_int), dp]),
         "scft_copy_fields": (C.c_int, [vp, vp]),
+        "scft_group_create": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(vp)]),
+        "scft_group_destroy": (None, [vp]),
+        "scft_group_last_error": (C.c_char_p, [vp]),
+        "scft_group_iterate": (C.c_int, [vp, C.c_int]),
+        "scft_group_time_iterations": (C.c_int, [vp, C.c_int, dp]),
+        "scft_group_launch_count": (C.c_longlong, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -303,3 +310,50 @@ class Context:
 
     def write_pha_dat(self, path: str, inst: int = 0):
         self._ck(self.lib.scft_write_pha_dat(self.h, path.encode(), inst))
+
+
+class Group:
+    """Heterogeneous batched sweep over several contexts (scft_group): one
+    CUDA-graph launch per iteration advances every member."""
+
+    def __init__(self, members):
+        self.lib = load_library()
+        self.members = list(members)          # keep the contexts alive
+        arr = (C.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+        h = C.c_void_p()
+        st = self.lib.scft_group_create(arr, len(self.members), C.byref(h))
+        if st != OK:
+            raise ScftError(st, self.lib.scft_last_error(None).decode())
+        self.h = h
+
+    def _ck(self, st):
+        if st != OK:
+            raise ScftError(st, self.lib.scft_group_last_error(self.h).decode())
+
+    def iterate(self, n: int):
+        self._ck(self.lib.scft_group_iterate(self.h, n))
+
+    def time_iterations(self, n: int) -> float:
+        ms = C.c_double()
+        self._ck(self.lib.scft_group_time_iterations(self.h, n, C.byref(ms)))
+        return ms.value
+
+    def launch_count(self) -> int:
+        return int(self.lib.scft_group_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.scft_group_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -231,7 +231,7 @@ int march_phase(scft_ctx *ctx, cudaStream_t st) {
 // and step counts of a context never change), so one launch replays the
 // ~3*(NsA+dNsB) kernels of the phase.
 int march_phase_graph(scft_ctx *ctx) {
-  if (!ctx->use_graph) return march_phase(ctx, ctx->st);
+  if (!ctx->use_graph || ctx->capturing) return march_phase(ctx, ctx->st);
   if (!ctx->march_exec) {
     const long long l0 = ctx->launches;
     CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
@@ -430,11 +430,16 @@ int read_fe(scft_ctx *ctx, double *out5) {
   return SCFT_OK;
 }
 
-int iterate_once(scft_ctx *ctx) {
+int pre_mix(scft_ctx *ctx) {
   int rc;
   if ((rc = average(ctx, ctx->wa))) return rc;   // cuda_scft.cu:170
   if ((rc = average(ctx, ctx->wb))) return rc;   // :172
-  if ((rc = get_conc(ctx))) return rc;           // :174
+  return get_conc(ctx);                          // :174
+}
+
+int iterate_once(scft_ctx *ctx) {
+  int rc = pre_mix(ctx);
+  if (rc) return rc;
   return mix(ctx);                               // :182
 }
 
@@ -463,6 +468,10 @@ void free_all(scft_ctx *ctx) {
 }
 
 }  // namespace
+
+// Hooks for the group graph (group.cu).
+int scft_internal_pre_mix(scft_ctx *ctx) { return pre_mix(ctx); }
+int scft_internal_mix(scft_ctx *ctx) { return mix(ctx); }
 
 int scft_fail(scft_ctx *ctx, int status, const std::string &msg) {
   if (ctx) ctx->err = msg;

@@ -17,6 +17,7 @@ struct scft_ctx {
   int rbytes = 8;               // sizeof working real (4 or 8)
   cudaStream_t st = nullptr;    // the context's stream (every launch)
   bool use_graph = true;        // march phase replayed as a CUDA graph
+  bool capturing = false;       // inside a group graph capture: launch directly
   bool use_pipe = false;        // persistent pipelined column passes (opt-in)
   bool two_streams = false;     // march chains on two forked streams instead of lockstep
   bool fuse_xy = false;         // x and y passes fused into one plane kernel (FP32)
