@@ -84,6 +84,7 @@ typedef struct scft_params {
 #define SCFT_FLAG_TWO_STREAMS 4   /* march chains on two forked streams (default when batch*M >= 2^20) */
 #define SCFT_FLAG_LOCKSTEP 8      /* march chains in shared lockstep launches (default below 2^20 points) */
 #define SCFT_FLAG_NO_XY 16        /* separate x and y passes instead of the fused plane kernel */
+#define SCFT_FLAG_AUTOTUNE 32     /* time every legal schedule at creation and keep the fastest */
 
 /* Fill *p with the reference defaults (32^3, box 4, xN 20, fa 0.5,
  * ds0 0.01, batch 1, FP64, simple mixing wopt 0.05 wcmp 0.10). */
@@ -164,6 +165,11 @@ int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir);
 
 /* Wait for all work queued on the context's stream. */
 int scft_synchronize(scft_ctx *ctx);
+
+/* The march schedule in use, as the SCFT_FLAG_* bits that select it
+ * (TWO_STREAMS or LOCKSTEP, NO_XY, PIPE), and -- after SCFT_FLAG_AUTOTUNE --
+ * the measured milliseconds of one march phase with it (else 0). */
+int scft_get_schedule(const scft_ctx *ctx, int *flags, double *march_ms);
 
 /* ---- convergence (no reference counterpart: the reference always runs
  * MaxIT iterations, cuda_scft.cu:253) ----

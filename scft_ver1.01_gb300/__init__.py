@@ -39,8 +39,10 @@ EXPORTS = [
     "scft_split_step_noalloc", "scft_noalloc_last_error", "scft_get_residual", "scft_converge",
     "scft_copy_fields", "scft_group_create", "scft_group_destroy", "scft_group_last_error",
     "scft_group_iterate", "scft_group_time_iterations", "scft_group_launch_count",
+    "scft_get_schedule",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
+FLAG_AUTOTUNE = 32
 
 
 class ScftParams(C.Structure):
@@ -117,6 +119,7 @@ def load_library(path: str | None = None):
         "scft_group_iterate": (C.c_int, [vp, C.c_int]),
         "scft_group_time_iterations": (C.c_int, [vp, C.c_int, dp]),
         "scft_group_launch_count": (C.c_longlong, [vp]),
+        "scft_get_schedule": (C.c_int, [vp, C.POINTER(C.c_int), dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -273,6 +276,12 @@ class Context:
 
     def launch_count(self) -> int:
         return int(self.lib.scft_launch_count(self.h))
+
+    def schedule(self):
+        """-> (SCFT_FLAG_* bits of the march schedule in use, autotuned march ms or 0)."""
+        f, ms = C.c_int(), C.c_double()
+        self._ck(self.lib.scft_get_schedule(self.h, C.byref(f), C.byref(ms)))
+        return f.value, ms.value
 
     def residual(self):
         """-> (err_max[batch], err_rms[batch]) of the last field update."""

@@ -469,6 +469,63 @@ void free_all(scft_ctx *ctx) {
 
 }  // namespace
 
+// Schedule autotuner: every legal combination of chain schedule (lockstep /
+// two streams), x+y fusion and column-pass kernel (one tile per CTA /
+// persistent pipelined) is captured and timed on the real march phase (three
+// replays after a warm-up, minimum taken); the fastest stays.  The fields are
+// whatever the context holds (timings do not depend on their values).
+int autotune(scft_ctx *ctx) {
+  bool has_fast_col = false;
+  for (size_t i = 1; i < ctx->passes.size(); ++i) has_fast_col |= ctx->passes[i].use_fast != 0;
+  const bool can_xy = ctx->fuse_xy;
+  int rc;
+  if ((rc = boltzmann(ctx, SCFT_FIELD_WA, ctx->st))) return rc;
+  if ((rc = boltzmann(ctx, SCFT_FIELD_WB, ctx->st))) return rc;
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  double best = 1e300;
+  bool best_two = ctx->two_streams, best_xy = ctx->fuse_xy, best_pipe = ctx->use_pipe;
+  for (int two = 0; two < 2; ++two)
+    for (int xy = 0; xy < (can_xy ? 2 : 1); ++xy)
+      for (int pipe = 0; pipe < (has_fast_col ? 2 : 1); ++pipe) {
+        ctx->two_streams = two;
+        ctx->fuse_xy = can_xy && xy;
+        ctx->use_pipe = pipe;
+        if (ctx->march_exec) cudaGraphExecDestroy(ctx->march_exec);
+        ctx->march_exec = nullptr;
+        if ((rc = march_phase_graph(ctx))) break;   // capture + warm-up
+        double ms = 1e300;
+        for (int r = 0; r < 3 && !rc; ++r) {
+          cudaEventRecord(a, ctx->st);
+          rc = march_phase_graph(ctx);
+          cudaEventRecord(b, ctx->st);
+          cudaEventSynchronize(b);
+          float f = 0.f;
+          cudaEventElapsedTime(&f, a, b);
+          if (f < ms) ms = f;
+        }
+        if (rc) break;
+        if (ms < best) {
+          best = ms;
+          best_two = two;
+          best_xy = ctx->fuse_xy;
+          best_pipe = pipe;
+        }
+      }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  ctx->two_streams = best_two;
+  ctx->fuse_xy = best_xy;
+  ctx->use_pipe = best_pipe;
+  if (ctx->march_exec) cudaGraphExecDestroy(ctx->march_exec);
+  ctx->march_exec = nullptr;
+  ctx->tuned_ms = best;
+  ctx->launches = 0;
+  return sync_check(ctx);
+}
+
 // Hooks for the group graph (group.cu).
 int scft_internal_pre_mix(scft_ctx *ctx) { return pre_mix(ctx); }
 int scft_internal_mix(scft_ctx *ctx) { return mix(ctx); }
@@ -531,7 +588,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   for (size_t i = 0; i < sizeof(p.reserved) / sizeof(p.reserved[0]); ++i)
     if (p.reserved[i]) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "reserved fields must be 0");
   if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_PIPE | SCFT_FLAG_TWO_STREAMS |
-                  SCFT_FLAG_LOCKSTEP | SCFT_FLAG_NO_XY))
+                  SCFT_FLAG_LOCKSTEP | SCFT_FLAG_NO_XY | SCFT_FLAG_AUTOTUNE))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad flags");
   if (!(p.lx > 0 && p.ly > 0 && p.lz > 0 && p.ds0 > 0 && p.fA >= 0 && p.fA <= 1 && p.batch >= 1))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
@@ -693,6 +750,10 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     return fail(SCFT_ERR_CUDA, "table upload failed");
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(SCFT_ERR_CUDA, "set-up failed");
   ctx->err = "no error";
+  if (p.flags & SCFT_FLAG_AUTOTUNE) {
+    const int rc = autotune(ctx);
+    if (rc) return fail(rc, "autotune: " + ctx->err);
+  }
   *out = ctx;
   return SCFT_OK;
 }
@@ -850,6 +911,15 @@ int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir) {
 int scft_synchronize(scft_ctx *ctx) {
   if (!ctx) return SCFT_ERR_INVALID_ARG;
   return sync_check(ctx);
+}
+
+int scft_get_schedule(const scft_ctx *ctx, int *flags, double *march_ms) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  if (flags)
+    *flags = (ctx->two_streams ? SCFT_FLAG_TWO_STREAMS : SCFT_FLAG_LOCKSTEP) |
+             (ctx->fuse_xy ? 0 : SCFT_FLAG_NO_XY) | (ctx->use_pipe ? SCFT_FLAG_PIPE : 0);
+  if (march_ms) *march_ms = ctx->tuned_ms;
+  return SCFT_OK;
 }
 
 int scft_get_residual(scft_ctx *ctx, double *err_max, double *err_rms) {

@@ -43,6 +43,28 @@ def test_group_equals_individual(pkg, mixing):
         ctx.close()
 
 
+@pytest.mark.parametrize("grid", [(64, 64, 64), (128, 64, 32)])
+def test_autotuned_schedule_gives_same_results(pkg, grid):
+    from scft_gb300 import fields
+    nx, ny, nz = grid
+    kw = dict(nx=nx, ny=ny, nz=nz, lx=4.0, ly=4.0, lz=4.0, hAB=18.0, fA=0.36, ds0=0.01,
+              precision=pkg.PREC_FP32)
+    wa, wb = fields.gyroid(nx, ny, nz, 4.0, 4.0, 4.0, 18.0, seed=2)
+    out = []
+    for flags in (0, pkg.FLAG_AUTOTUNE):
+        with pkg.Context(flags=flags, **kw) as ctx:
+            sched, ms = ctx.schedule()
+            assert bool(sched & pkg.FLAG_TWO_STREAMS) != bool(sched & pkg.FLAG_LOCKSTEP)
+            if flags:
+                assert ms > 0
+            ctx.set_w(wa, wb)
+            ctx.iterate(2)
+            out.append(ctx.pha)
+    # schedules only reorder independent work: identical kernels per pass type,
+    # so the results agree to FP32 round-off of the differing pass kernels
+    assert np.abs(out[0] - out[1]).max() < 2e-5 * np.abs(out[0]).max()
+
+
 def test_group_rejects_duplicates(pkg):
     kw = MEMBERS[0]
     with pkg.Context(**kw) as ctx:
