@@ -52,6 +52,8 @@ extern "C" {
 
 #define SCFT_MIX_SIMPLE 0         /* phi_w (cuda_aid.cu:382-416) */
 #define SCFT_MIX_ANDERSON 1       /* Anderson mixing on the phi_w residual (no reference counterpart) */
+#define SCFT_MIX_CONSTRAINED 2    /* phi_w_constrained toward a target phiA (cuda_aid.cu:418-452) */
+#define SCFT_MIX_CONSTRAINED_EX 3 /* phi_w_constrainedEx toward a target phiA (cuda_aid.cu:454-490) */
 
 typedef struct scft_ctx scft_ctx;
 
@@ -74,7 +76,8 @@ typedef struct scft_params {
   int device;               /* CUDA device ordinal */
   int flags;                /* SCFT_FLAG_* */
   double anderson_start;    /* simple mixing until the residual max-norm drops below this */
-  int reserved[5];          /* must be zero */
+  double constraint_lambda; /* penalty weight of SCFT_MIX_CONSTRAINED (phi_w_constrained's lambda) */
+  int reserved[4];          /* must be zero */
 } scft_params;
 
 /* flags */
@@ -258,6 +261,24 @@ int scft_read_phi_dat(scft_ctx *ctx, const char *path, int inst);
 
 /* Write pha_<idx>.dat (cuda_scft.cu:233-243) for instance `inst`. */
 int scft_write_pha_dat(scft_ctx *ctx, const char *path, int inst);
+
+/* Write phiA - phiB of instance `inst` as the ASCII STRUCTURED_POINTS file of
+ * the reference's converter (vtk.c:54-76); `source` names the data in the
+ * comment line (vtk.c:55). */
+int scft_write_vtk(scft_ctx *ctx, const char *path, int inst, const char *source);
+
+/* The reference's converter itself (vtk.c:4-81): pha_<i>.dat file -> VTK file. */
+int scft_convert_pha_to_vtk(const char *pha_path, const char *vtk_path);
+
+/* Target phiA field of the constrained updates ([batch][Nz][Ny][Nx] host
+ * doubles, the reference's PhA_cu, cuda_aid.cu:418). */
+int scft_set_target(scft_ctx *ctx, const double *pha_target);
+
+/* One constrained field update on the current fields:
+ * phi_w_constrained (cuda_aid.cu:418-452; constants wopt 0.05, wcmp 0.10,
+ * penalty `lambda`) when ex == 0, phi_w_constrainedEx (cuda_aid.cu:454-490;
+ * wopt 1.60, wcmp 0.50) when ex != 0. */
+int scft_phi_w_constrained(scft_ctx *ctx, int ex, double lambda);
 
 #ifdef __cplusplus
 }

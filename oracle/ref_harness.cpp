@@ -31,11 +31,13 @@ struct Ref {
   int thread = 1, thread_sur = 1;
   CUmodule mod = nullptr;
   CUfunction f_wdz, f_q, f_qinv, f_in_go, f_sur_go, f_in_to_g_go, f_qint_init, f_qa_to_qint,
-      f_qa_to_qint2, f_cal_ql, f_w_to_phi_go, f_minus_average, f_phi_w, f_reduce3;
+      f_qa_to_qint2, f_cal_ql, f_w_to_phi_go, f_minus_average, f_phi_w, f_reduce3,
+      f_phi_w_con, f_phi_w_con_ex;
   cufftHandle plan_f = 0, plan_b = 0;
   double *kxyzdz = nullptr, *wa = nullptr, *wb = nullptr, *pha = nullptr, *phb = nullptr,
          *qint = nullptr, *wdz = nullptr, *qa = nullptr, *qca = nullptr, *qb = nullptr,
-         *qcb = nullptr, *ql = nullptr, *ffl = nullptr, *in = nullptr, *sum = nullptr;
+         *qcb = nullptr, *ql = nullptr, *ffl = nullptr, *in = nullptr, *sum = nullptr,
+         *target = nullptr;
   cufftDoubleComplex *out = nullptr;
   std::vector<double> hql, hql_raw;
   int q_mode = 1;
@@ -216,11 +218,24 @@ int phi_w() {
   return 0;
 }
 
+// phi_w_constrained / phi_w_constrainedEx (cuda_aid.cu:418-490), launched
+// with phi_w's geometry; the reference has no call site for them.
+int phi_w_constrained(int ex, double lambda) {
+  if (!g.target) return fail("no target field");
+  void *a[] = {&g.wa, &g.wb, &g.pha, &g.phb, &g.target, &g.hAB, &lambda};   // Ex: no lambda
+  void *a_ex[] = {&g.wa, &g.wb, &g.pha, &g.phb, &g.target, &g.hAB};
+  if (launch(ex ? g.f_phi_w_con_ex : g.f_phi_w_con, dim3(g.nx, g.ny, g.nz), dim3(g.batch), 0,
+             ex ? a_ex : a))
+    return 1;
+  CR(cudaDeviceSynchronize());
+  return 0;
+}
+
 void release() {
   cudaFree(g.kxyzdz); cudaFree(g.wa); cudaFree(g.wb); cudaFree(g.pha); cudaFree(g.phb);
   cudaFree(g.qint); cudaFree(g.wdz); cudaFree(g.qa); cudaFree(g.qca); cudaFree(g.qb);
   cudaFree(g.qcb); cudaFree(g.ql); cudaFree(g.ffl); cudaFree(g.in); cudaFree(g.out);
-  cudaFree(g.sum);
+  cudaFree(g.sum); cudaFree(g.target);
   if (g.plan_f) cufftDestroy(g.plan_f);
   if (g.plan_b) cufftDestroy(g.plan_b);
   if (g.mod) cuModuleUnload(g.mod);
@@ -259,7 +274,8 @@ int ref_open(const char *cubin, int nx, int ny, int nz, double lx, double ly, do
       {"qInt_init", &g.f_qint_init}, {"10qa_to_qInt", &g.f_qa_to_qint},
       {"qa_to_qInt2", &g.f_qa_to_qint2}, {"cal_ql", &g.f_cal_ql},
       {"w_to_phi_go", &g.f_w_to_phi_go}, {"minus_average", &g.f_minus_average},
-      {"5phi_w", &g.f_phi_w}, {"reduce3", &g.f_reduce3}};
+      {"5phi_w", &g.f_phi_w}, {"reduce3", &g.f_reduce3},
+      {"17phi_w_constrained", &g.f_phi_w_con}, {"19phi_w_constrainedEx", &g.f_phi_w_con_ex}};
   for (auto &k : ks)
     if (find_kernel(k.n, k.f)) return 1;
   int dim[3] = {nz, ny, nx};   // init_cuda.cu:345
@@ -375,6 +391,12 @@ int ref_get_q(int which, int s, double *dst) {
 int ref_average_value(int which) { return average_value(which == 0 ? g.wa : g.wb); }
 int ref_get_conc() { return get_conc(); }
 int ref_phi_w() { return phi_w(); }
+int ref_set_target(const double *src) {
+  if (!g.target) CR(cudaMalloc(&g.target, sizeof(double) * g.M * g.batch));
+  CR(cudaMemcpy(g.target, src, sizeof(double) * g.M * g.batch, cudaMemcpyHostToDevice));
+  return 0;
+}
+int ref_phi_w_constrained(int ex, double lambda) { return phi_w_constrained(ex, lambda); }
 
 // n iterations of the Free loop body (cuda_scft.cu:167-186); after the last
 // one, the free-energy block (:190-221) on the host: out5[b] = {F, FAB, FW, FS, inc}.

@@ -37,6 +37,8 @@ class RefSolver:
         L.ref_iterate.argtypes = [C.c_int, dp]
         L.ref_time_iterations.argtypes = [C.c_int, dp]
         L.ref_get_ns.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.ref_set_target.argtypes = [dp]
+        L.ref_phi_w_constrained.argtypes = [C.c_int, C.c_double]
         self._ck(L.ref_open(CUBIN.encode(), nx, ny, nz, lx, ly, lz, hAB, fA, ds0, batch))
         a, b = C.c_int(), C.c_int()
         L.ref_get_ns(C.byref(a), C.byref(b))
@@ -82,6 +84,13 @@ class RefSolver:
 
     def phi_w(self):
         self._ck(self.lib.ref_phi_w())
+
+    def set_target(self, pha_target):
+        a = np.ascontiguousarray(pha_target, dtype=np.float64).reshape(self.shape)
+        self._ck(self.lib.ref_set_target(self._p(a)))
+
+    def phi_w_constrained(self, ex=False, lam=0.0):
+        self._ck(self.lib.ref_phi_w_constrained(int(bool(ex)), C.c_double(lam)))
 
     def iterate(self, n, with_energy=True):
         out = np.empty((self.shape[0], 5))

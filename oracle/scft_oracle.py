@@ -256,6 +256,64 @@ def phi_w(wa, wb, pha, phb, hAB, wopt=0.05, wcmp=0.10):
     return wa + wopt * wad, wb + wopt * wbd, wad, wbd
 
 
+def phi_w_constrained(wa, wb, pha, phb, target, hAB, lam):
+    """``phi_w_constrained`` (cuda_aid.cu:418-452): phi_w plus a penalty
+    lam*(phiA - target) on wA and lam*(phiB - (1 - target)) on wB, with the
+    kernel's own wopt 0.05 and wcmp 0.10."""
+    wopt, wcmp = 0.050, 0.10
+    eta = (wa + wb - hAB) / 2
+    psum = 1.0 - pha - phb
+    wad = hAB * phb + eta - wa + lam * (pha - target)
+    wbd = hAB * pha + eta - wb + lam * (phb - (1 - target))
+    wad = wad - wcmp * psum
+    wbd = wbd - wcmp * psum
+    return wa + wopt * wad, wb + wopt * wbd
+
+
+def phi_w_constrained_ex(wa, wb, pha, phb, target, hAB):
+    """``phi_w_constrainedEx`` (cuda_aid.cu:454-490): the exchange-field form
+    with wum = -hAB(2 target - 1) - (wA - wB) and the kernel's own wopt 1.60,
+    wcmp 0.50."""
+    wopt, wcmp = 1.60, 0.50
+    wum = -hAB * (target * 2 - 1) - (wa - wb)
+    eta = (wa + wb - hAB + wum) / 2
+    psum = 1.0 - pha - phb
+    psum1 = pha - target
+    wad = hAB * (1 - target) + eta - wa - wum
+    wbd = hAB * target + eta - wb
+    wad = wad - (2.0 * wcmp * psum - 2.0 * wcmp * psum1)
+    wbd = wbd - 2 * wcmp * psum1
+    return wa + wopt * wad, wb + wopt * wbd
+
+
+def vtk_text(source, nx, ny, nz, dx, dy, dz, diff):
+    """Text of the converter's output (vtk.c:54-76): header, then phiA - phiB
+    as ``%7.4lf `` per point with x fastest and one line per (z, y) row."""
+    out = ["# vtk DataFile Version 3.0\n",
+           "# comment: converted from file %s\n" % source,
+           "ASCII\n", "DATASET STRUCTURED_POINTS\n",
+           "DIMENSIONS %d %d %d\n" % (nx, ny, nz),
+           "ORIGIN 0.000000 0.000000 0.000000\n",
+           "SPACING %.6f %.6f %.6f\n\n" % (dx, dy, dz),
+           "POINT_DATA %d\n" % (nx * ny * nz),
+           "SCALARS scalars float\n", "LOOKUP_TABLE default\n\n"]
+    d = np.asarray(diff, dtype=np.float64).reshape(nz * ny, nx)
+    for row in d:
+        out.append("".join("%7.4f " % v for v in row) + "\n")
+    return "".join(out)
+
+
+def convert_pha_to_vtk(pha_path, source=None):
+    """The converter (vtk.c:4-81) on a pha file: returns the VTK text."""
+    with open(pha_path) as f:
+        h1 = f.readline()
+        h2 = f.readline()
+        nx, ny, nz = (int(t.split("=")[1]) for t in h1.strip().split(","))
+        dx, dy, dz = (float(t.split("=")[1]) for t in h2.strip().split(","))
+        data = np.loadtxt(f, max_rows=nx * ny * nz).reshape(-1, 4)
+    return vtk_text(source or pha_path, nx, ny, nz, dx, dy, dz, data[:, 0] - data[:, 1])
+
+
 def free_energy(wa, wb, pha, phb, Q, hAB):
     """The free-energy block of ``Free`` (cuda_scft.cu:190-221), per instance:
     returns (F, F_AB, F_W, F_S, inCompMax)."""

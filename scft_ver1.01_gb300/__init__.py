@@ -26,7 +26,7 @@ ERR_NOT_FINITE, ERR_IO, ERR_NO_DEVICE = 5, 6, 7
 PREC_FP64, PREC_FP32 = 0, 1
 FIELD_WA, FIELD_WB, FIELD_PHA, FIELD_PHB = 0, 1, 2, 3
 Q_A, Q_CB, Q_B, Q_CA = 0, 1, 2, 3
-MIX_SIMPLE, MIX_ANDERSON = 0, 1
+MIX_SIMPLE, MIX_ANDERSON, MIX_CONSTRAINED, MIX_CONSTRAINED_EX = 0, 1, 2, 3
 
 # Every symbol include/scft_capi.h declares (checked by the CPU tests).
 EXPORTS = [
@@ -39,7 +39,8 @@ EXPORTS = [
     "scft_split_step_noalloc", "scft_noalloc_last_error", "scft_get_residual", "scft_converge",
     "scft_copy_fields", "scft_group_create", "scft_group_destroy", "scft_group_last_error",
     "scft_group_iterate", "scft_group_time_iterations", "scft_group_launch_count",
-    "scft_get_schedule",
+    "scft_get_schedule", "scft_write_vtk", "scft_convert_pha_to_vtk", "scft_set_target",
+    "scft_phi_w_constrained",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
 FLAG_AUTOTUNE = 32
@@ -55,7 +56,7 @@ class ScftParams(C.Structure):
         ("wopt", C.c_double), ("wcmp", C.c_double),
         ("mixing", C.c_int), ("anderson_history", C.c_int), ("anderson_lambda", C.c_double),
         ("device", C.c_int), ("flags", C.c_int), ("anderson_start", C.c_double),
-        ("reserved", C.c_int * 5),
+        ("constraint_lambda", C.c_double), ("reserved", C.c_int * 4),
     ]
 
 
@@ -120,6 +121,10 @@ def load_library(path: str | None = None):
         "scft_group_time_iterations": (C.c_int, [vp, C.c_int, dp]),
         "scft_group_launch_count": (C.c_longlong, [vp]),
         "scft_get_schedule": (C.c_int, [vp, C.POINTER(C.c_int), dp]),
+        "scft_write_vtk": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_char_p]),
+        "scft_convert_pha_to_vtk": (C.c_int, [C.c_char_p, C.c_char_p]),
+        "scft_set_target": (C.c_int, [vp, dp]),
+        "scft_phi_w_constrained": (C.c_int, [vp, C.c_int, C.c_double]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -150,6 +155,14 @@ def read_ab_txt(path: str):
     if st != OK:
         raise ScftError(st, lib.scft_last_error(None).decode())
     return p, tag.value
+
+
+def convert_pha_to_vtk(pha_path: str, vtk_path: str):
+    """The reference's pha file -> VTK converter (vtk.c)."""
+    lib = load_library()
+    st = lib.scft_convert_pha_to_vtk(pha_path.encode(), vtk_path.encode())
+    if st != OK:
+        raise ScftError(st, lib.scft_last_error(None).decode())
 
 
 def _dptr(a: np.ndarray):
@@ -319,6 +332,19 @@ class Context:
 
     def write_pha_dat(self, path: str, inst: int = 0):
         self._ck(self.lib.scft_write_pha_dat(self.h, path.encode(), inst))
+
+    def write_vtk(self, path: str, inst: int = 0, source: str = "pha.dat"):
+        """phiA - phiB of one instance as the reference converter's VTK file."""
+        self._ck(self.lib.scft_write_vtk(self.h, path.encode(), inst, source.encode()))
+
+    def set_target(self, pha_target: np.ndarray):
+        """Target phiA of the constrained updates ([batch, Nz, Ny, Nx] or [Nz, Ny, Nx])."""
+        a = np.ascontiguousarray(np.broadcast_to(pha_target, self.shape), dtype=np.float64)
+        self._ck(self.lib.scft_set_target(self.h, _dptr(a)))
+
+    def phi_w_constrained(self, ex: bool = False, lam: float = 0.0):
+        """One phi_w_constrained (ex False) or phi_w_constrainedEx (ex True) update."""
+        self._ck(self.lib.scft_phi_w_constrained(self.h, int(bool(ex)), lam))
 
 
 class Group:

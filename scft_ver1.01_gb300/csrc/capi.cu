@@ -365,6 +365,20 @@ int get_conc(scft_ctx *ctx) {
 int mix(scft_ctx *ctx) {
   const long long M = ctx->M;
   const int B = ctx->batch;
+  if (ctx->p.mixing == SCFT_MIX_CONSTRAINED || ctx->p.mixing == SCFT_MIX_CONSTRAINED_EX) {
+    // the residual of the free update (for convergence reports), then the
+    // constrained step
+    if (!ctx->target)
+      return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "constrained mixing needs a target field");
+    CKL(scft::launch_residual(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->p.wcmp, 0.0,
+                              M, B, nullptr, nullptr, ctx->rpartial, ctx->nblk, ctx->res,
+                              ctx->st));
+    CKL(scft::launch_phi_w_constrained(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->target,
+                                       ctx->p.hAB, ctx->p.constraint_lambda,
+                                       ctx->p.mixing == SCFT_MIX_CONSTRAINED_EX, M, B, ctx->st));
+    ctx->launches += 3;
+    return SCFT_OK;
+  }
   if (ctx->p.mixing == SCFT_MIX_SIMPLE) {
     CKL(scft::launch_residual(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->p.wcmp,
                               ctx->p.wopt, M, B, nullptr, nullptr, ctx->rpartial, ctx->nblk,
@@ -457,7 +471,7 @@ void free_all(scft_ctx *ctx) {
   cudaFree(ctx->partial); cudaFree(ctx->sum); cudaFree(ctx->Q); cudaFree(ctx->ffl);
   cudaFree(ctx->fe5); cudaFree(ctx->tables); cudaFree(ctx->dev_err);
   cudaFree(ctx->res); cudaFree(ctx->rpartial); cudaFree(ctx->gram); cudaFree(ctx->and_a);
-  cudaFree(ctx->and_lam);
+  cudaFree(ctx->and_lam); cudaFree(ctx->target);
   for (double *h : ctx->hist_w) cudaFree(h);
   for (double *h : ctx->hist_d) cudaFree(h);
   ctx->hist_w.clear();
@@ -594,7 +608,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
   if (p.precision != SCFT_PREC_FP64 && p.precision != SCFT_PREC_FP32)
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad precision");
-  if (p.mixing != SCFT_MIX_SIMPLE && p.mixing != SCFT_MIX_ANDERSON)
+  if (p.mixing < SCFT_MIX_SIMPLE || p.mixing > SCFT_MIX_CONSTRAINED_EX)
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad mixing mode");
   if (p.mixing == SCFT_MIX_ANDERSON &&
       (p.anderson_history < 1 || p.anderson_history > 32 || !(p.anderson_lambda > 0)))
@@ -859,6 +873,24 @@ int scft_get_Q(scft_ctx *ctx, double *dst) {
 int scft_phi_w(scft_ctx *ctx) {
   if (!ctx) return SCFT_ERR_INVALID_ARG;
   return mix(ctx);
+}
+
+int scft_set_target(scft_ctx *ctx, const double *pha_target) {
+  if (!ctx || !pha_target) return SCFT_ERR_INVALID_ARG;
+  CK(cudaSetDevice(ctx->p.device));
+  const size_t bytes = sizeof(double) * ctx->M * ctx->batch;
+  if (!ctx->target) CK(cudaMalloc((void **)&ctx->target, bytes));
+  CK(cudaMemcpyAsync(ctx->target, pha_target, bytes, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return SCFT_OK;
+}
+
+int scft_phi_w_constrained(scft_ctx *ctx, int ex, double lambda) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  if (!ctx->target) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "no target field set");
+  CKL(scft::launch_phi_w_constrained(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->target,
+                                     ctx->p.hAB, lambda, ex != 0, ctx->M, ctx->batch, ctx->st));
+  return SCFT_OK;
 }
 
 int scft_free_energy(scft_ctx *ctx, double *out5) {

@@ -51,6 +51,7 @@ struct scft_ctx {
   double *and_a = nullptr;        // [batch][m1] slot weights
   double *and_lam = nullptr;      // [batch] step
   long long and_count = 0;        // iterations stored in the ring
+  double *target = nullptr;       // [batch][M] target phiA of the constrained updates
   // spectral tables (twiddles + gains of each pass), device
   void *tables = nullptr;
   std::vector<scft::AxisPlan> passes;

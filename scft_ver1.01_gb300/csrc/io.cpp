@@ -1,8 +1,9 @@
 // Drop-in file formats of the reference: ab.txt (init.cpp:81-94),
-// phi_<i>.dat input (init_cuda.cu:435-456) and pha_<i>.dat output
-// (cuda_scft.cu:233-243).  Unlike the reference, a missing or malformed file
+// phi_<i>.dat input (init_cuda.cu:435-456), pha_<i>.dat output
+// (cuda_scft.cu:233-243) and the VTK converter's output (vtk.c).  Unlike the reference, a missing or malformed file
 // is reported as SCFT_ERR_IO instead of crashing on fscanf(NULL).
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <string>
@@ -85,6 +86,108 @@ int scft_write_pha_dat(scft_ctx *ctx, const char *path, int inst) {
           p.lz / (double)p.nz);
   for (long long i = 0; i < M; ++i) fprintf(dp, "%g %g %g %g\n", a[i], b[i], c[i], d[i]);
   fclose(dp);
+  return SCFT_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The converter's output (vtk.c:54-76): a STRUCTURED_POINTS header with the
+// spacing as read, then phiA - phiB as "%7.4lf " per point, x fastest, one
+// text row per (z, y).  `diff` holds nx*ny*nz values in that order.
+int write_vtk_file(const char *path, const char *source, int nx, int ny, int nz, double dx,
+                   double dy, double dz, const std::vector<double> &diff) {
+  FILE *fp = fopen(path, "w");
+  if (!fp) return SCFT_ERR_IO;
+  fprintf(fp, "# vtk DataFile Version 3.0\n");
+  fprintf(fp, "# comment: converted from file %s\n", source);
+  fprintf(fp, "ASCII\n");
+  fprintf(fp, "DATASET STRUCTURED_POINTS\n");
+  fprintf(fp, "DIMENSIONS %d %d %d\n", nx, ny, nz);
+  fprintf(fp, "ORIGIN 0.000000 0.000000 0.000000\n");
+  fprintf(fp, "SPACING %.6f %.6f %.6f\n\n", dx, dy, dz);
+  fprintf(fp, "POINT_DATA %lld\n", (long long)nx * ny * nz);
+  fprintf(fp, "SCALARS scalars float\n");
+  fprintf(fp, "LOOKUP_TABLE default\n\n");
+  // one row buffered at a time: a 128^3 field is 16K rows of 8*nx bytes
+  std::string row;
+  char cell[64];
+  long long i = 0;
+  for (long long r = 0; r < (long long)ny * nz; ++r) {
+    row.clear();
+    for (int x = 0; x < nx; ++x, ++i) {
+      snprintf(cell, sizeof cell, "%7.4f ", diff[i]);
+      row += cell;
+    }
+    row += '\n';
+    fwrite(row.data(), 1, row.size(), fp);
+  }
+  return fclose(fp) == 0 ? SCFT_OK : SCFT_ERR_IO;
+}
+
+// A value as it survives the pha file's "%g" text (cuda_scft.cu:238).
+double through_g(double v) {
+  char t[64];
+  snprintf(t, sizeof t, "%g", v);
+  return strtod(t, nullptr);
+}
+
+}  // namespace
+
+extern "C" {
+
+int scft_convert_pha_to_vtk(const char *pha_path, const char *vtk_path) {
+  const char *in = pha_path ? pha_path : "pha.dat";     // vtk.c:17-18 defaults
+  const char *out = vtk_path ? vtk_path : "out.vtk";
+  FILE *fp = fopen(in, "r");
+  if (!fp) return scft_fail(nullptr, SCFT_ERR_IO, std::string("cannot open ") + in);
+  int nx = 0, ny = 0, nz = 0;
+  double dx = 0, dy = 0, dz = 0;
+  int n = fscanf(fp, "Nx=%d, Ny=%d, Nz=%d\n", &nx, &ny, &nz);
+  n += fscanf(fp, "dx=%lf, dy=%lf, dz=%lf\n", &dx, &dy, &dz);
+  if (n != 6 || nx <= 0 || ny <= 0 || nz <= 0) {
+    fclose(fp);
+    return scft_fail(nullptr, SCFT_ERR_IO, std::string("malformed header in ") + in);
+  }
+  const long long M = (long long)nx * ny * nz;
+  std::vector<double> diff(M);
+  for (long long i = 0; i < M; ++i) {
+    double a, b, c, d;
+    if (fscanf(fp, "%lf %lf %lf %lf\n", &a, &b, &c, &d) != 4) {
+      fclose(fp);
+      return scft_fail(nullptr, SCFT_ERR_IO, std::string("short or malformed field file ") + in);
+    }
+    diff[i] = a - b;
+  }
+  fclose(fp);
+  if (write_vtk_file(out, in, nx, ny, nz, dx, dy, dz, diff) != SCFT_OK)
+    return scft_fail(nullptr, SCFT_ERR_IO, std::string("cannot write ") + out);
+  return SCFT_OK;
+}
+
+int scft_write_vtk(scft_ctx *ctx, const char *path, int inst, const char *source) {
+  if (!ctx || !path) return SCFT_ERR_INVALID_ARG;
+  if (inst < 0 || inst >= ctx->batch) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad instance");
+  const long long M = ctx->M;
+  std::vector<double> a(M), b(M);
+  cudaSetDevice(ctx->p.device);
+  cudaError_t e = cudaStreamSynchronize(ctx->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(a.data(), ctx->pha + (long long)inst * M, sizeof(double) * M,
+                   cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b.data(), ctx->phb + (long long)inst * M, sizeof(double) * M,
+                   cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return scft_fail(ctx, SCFT_ERR_CUDA, cudaGetErrorString(e));
+  // the same values the pha file -> converter route gives: phiA and phiB as
+  // their "%g" text, the spacing as "%g" text
+  for (long long i = 0; i < M; ++i) a[i] = through_g(a[i]) - through_g(b[i]);
+  const scft_params &p = ctx->p;
+  if (write_vtk_file(path, source ? source : "pha.dat", p.nx, p.ny, p.nz,
+                     through_g(p.lx / (double)p.nx), through_g(p.ly / (double)p.ny),
+                     through_g(p.lz / (double)p.nz), a) != SCFT_OK)
+    return scft_fail(ctx, SCFT_ERR_IO, std::string("cannot write ") + path);
   return SCFT_OK;
 }
 

@@ -179,6 +179,52 @@ __global__ void k_phi_w(double *__restrict__ wa, double *__restrict__ wb,
   }
 }
 
+// phi_w_constrained (cuda_aid.cu:418-452): simple mixing plus a penalty
+// pulling phiA toward the target T with weight lambda; its constants are the
+// reference's hard-coded wopt 0.05, wcmp 0.10.
+__global__ void k_phi_w_constrained(double *__restrict__ wa, double *__restrict__ wb,
+                                    const double *__restrict__ pha,
+                                    const double *__restrict__ phb,
+                                    const double *__restrict__ tgt, double hAB, double lambda,
+                                    long long n) {
+  const double wopt = 0.050, wcmp = 0.10;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double a = wa[i], b = wb[i], pa = pha[i], pb = phb[i], t = tgt[i];
+    const double eta = (a + b - hAB) / 2;
+    const double psum = 1.0 - pa - pb;
+    double da = hAB * pb + eta - a + lambda * (pa - t);
+    double db = hAB * pa + eta - b + lambda * (pb - (1 - t));
+    da -= wcmp * psum;
+    db -= wcmp * psum;
+    wa[i] = a + wopt * da;
+    wb[i] = b + wopt * db;
+  }
+}
+
+// phi_w_constrainedEx (cuda_aid.cu:454-490): the exchange-field form with the
+// reference's hard-coded wopt 1.60, wcmp 0.50.
+__global__ void k_phi_w_constrained_ex(double *__restrict__ wa, double *__restrict__ wb,
+                                       const double *__restrict__ pha,
+                                       const double *__restrict__ phb,
+                                       const double *__restrict__ tgt, double hAB, long long n) {
+  const double wopt = 1.60, wcmp = 0.50;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double a = wa[i], b = wb[i], pa = pha[i], pb = phb[i], t = tgt[i];
+    const double wum = -hAB * (t * 2 - 1) - (a - b);
+    const double eta = (a + b - hAB + wum) / 2;
+    const double psum = 1.0 - pa - pb;
+    const double psum1 = pa - t;
+    double da = hAB * (1 - t) + eta - a - wum;
+    double db = hAB * t + eta - b;
+    da -= 2.0 * wcmp * psum - 2.0 * wcmp * psum1;
+    db -= 2 * wcmp * psum1;
+    wa[i] = a + wopt * da;
+    wb[i] = b + wopt * db;
+  }
+}
+
 // partial layout: [b][3][nblk]
 __global__ void k_fe_partials(const double *__restrict__ wa, const double *__restrict__ wb,
                               const double *__restrict__ pha, const double *__restrict__ phb,
@@ -299,6 +345,18 @@ cudaError_t launch_phi_w(double *wa, double *wb, const double *pha, const double
   k_phi_w<<<grid_for(n), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, wopt, wcmp, n);
   return cudaGetLastError();
 }
+cudaError_t launch_phi_w_constrained(double *wa, double *wb, const double *pha, const double *phb,
+                                     const double *target, double hAB, double lambda, int ex,
+                                     long long M, int batch, cudaStream_t st) {
+  const long long n = M * batch;
+  if (ex)
+    k_phi_w_constrained_ex<<<grid_for(n), kThreads, 0, st>>>(wa, wb, pha, phb, target, hAB, n);
+  else
+    k_phi_w_constrained<<<grid_for(n), kThreads, 0, st>>>(wa, wb, pha, phb, target, hAB, lambda,
+                                                           n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_free_energy_partials(const double *wa, const double *wb, const double *pha,
                                         const double *phb, double hAB, long long M, int batch,
                                         double *partial, int nblk, cudaStream_t st) {

@@ -120,6 +120,10 @@ cudaError_t launch_contour_phi(const R *q, const R *qc, int ns, long long M, int
 cudaError_t launch_phi_w(double *wa, double *wb, const double *pha, const double *phb,
                          double hAB, double wopt, double wcmp, long long M, int batch,
                          cudaStream_t st);
+// phi_w_constrained (ex == 0) / phi_w_constrainedEx (ex != 0)
+cudaError_t launch_phi_w_constrained(double *wa, double *wb, const double *pha, const double *phb,
+                                     const double *target, double hAB, double lambda, int ex,
+                                     long long M, int batch, cudaStream_t st);
 // free energy partials: sums of hAB*pa*pb, wa*pa+wb*pb and max|1-pa-pb|
 cudaError_t launch_free_energy_partials(const double *wa, const double *wb, const double *pha,
                                         const double *phb, double hAB, long long M, int batch,

@@ -97,6 +97,35 @@ def run_quirk(outdir):
     r.close()
 
 
+def run_constrained(outdir):
+    """phi_w_constrained (lambda 0.7) and phi_w_constrainedEx
+    (cuda_aid.cu:418-490) of the reference on seeded fields, batch 2."""
+    from oracle.ref_harness import RefSolver
+    grid, box, chiN, lam = (16, 12, 8), (3.0, 3.0, 2.0), 17.0, 0.7
+    rng = np.random.default_rng(23)
+    shape = (2,) + grid[::-1]
+    wa = rng.normal(0.0, 2.0, shape)
+    wb = rng.normal(0.0, 2.0, shape)
+    pha = rng.uniform(0.05, 0.95, shape)
+    phb = 1.0 - pha + rng.normal(0.0, 0.02, shape)
+    target = rng.uniform(0.0, 1.0, shape)
+    out = dict(grid=np.array(grid), box=np.array(box), chiN=chiN, lam=lam, wa_in=wa, wb_in=wb,
+               pha=pha, phb=phb, target=target)
+    r = RefSolver(*grid, *box, chiN, 0.5, 0.05, 2)
+    for key, ex in (("con", False), ("conex", True)):
+        r.set_w(wa, wb)
+        r.set_field(2, pha)
+        r.set_field(3, phb)
+        r.set_target(target)
+        r.phi_w_constrained(ex, lam)
+        out[key + "_wa"] = r.get_field(0)
+        out[key + "_wb"] = r.get_field(1)
+    r.close()
+    path = os.path.join(outdir, "ref_constrained16x12x8.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path)
+
+
 def time_reference():
     from oracle.ref_harness import RefSolver
     n, L = 128, 3.8
@@ -118,11 +147,18 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
     ap.add_argument("--time", action="store_true")
+    ap.add_argument("--only", nargs="*", default=None,
+                    help="case names to (re)generate (default: all); 'quirk12', 'constrained'")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
+    want = lambda n: args.only is None or n in args.only
     for c in CASES:
-        run_case(c, args.out)
-    run_quirk(args.out)
+        if want(c[0]):
+            run_case(c, args.out)
+    if want("quirk12"):
+        run_quirk(args.out)
+    if want("constrained"):
+        run_constrained(args.out)
     if args.time:
         time_reference()
 

@@ -8,7 +8,10 @@ import numpy as np
 import pytest
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = sorted(p for p in glob.glob(os.path.join(GOLD, "ref_*.npz")) if "quirk" not in p)
+# SCF cases (getConc + loop); the quirk, constrained-update and VTK fixtures
+# have their own tests
+CASES = sorted(p for p in glob.glob(os.path.join(GOLD, "ref_*.npz"))
+               if "loop_fe" in np.load(p).files)
 
 
 def rel(a, b):
@@ -66,3 +69,18 @@ def test_reduce3_quirk_matches_reference(orc):
     np.testing.assert_allclose(d["w_avg"], w - mean_quirk, rtol=0, atol=1e-13)
     # ... and it is not the true mean subtraction
     assert np.abs(d["w_avg"] - orc.average_value(w)).max() > 1e-6
+
+
+def test_constrained_updates_match_reference(orc):
+    """phi_w_constrained (lambda 0.7) and phi_w_constrainedEx run by the
+    reference's own kernels (cuda_aid.cu:418-490) on seeded fields."""
+    d = np.load(os.path.join(GOLD, "ref_constrained16x12x8.npz"))
+    chiN, lam = float(d["chiN"]), float(d["lam"])
+    args = (d["wa_in"], d["wb_in"], d["pha"], d["phb"], d["target"], chiN)
+    wa, wb = orc.phi_w_constrained(*args, lam)
+    assert rel(wa, d["con_wa"]) < 1e-14 and rel(wb, d["con_wb"]) < 1e-14
+    wa, wb = orc.phi_w_constrained_ex(*args)
+    assert rel(wa, d["conex_wa"]) < 1e-14 and rel(wb, d["conex_wb"]) < 1e-14
+    # the penalty term is really exercised
+    wa0, _ = orc.phi_w_constrained(*args, 0.0)
+    assert rel(wa0, d["con_wa"]) > 1e-3
