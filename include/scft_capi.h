@@ -280,6 +280,52 @@ int scft_set_target(scft_ctx *ctx, const double *pha_target);
  * wopt 1.60, wcmp 0.50) when ex != 0. */
 int scft_phi_w_constrained(scft_ctx *ctx, int ex, double lambda);
 
+/* ---- derivatives (no reference counterpart) ----------------------------
+ * F is the per-chain free energy of Free (cuda_scft.cu:190-221); the box
+ * lengths lx, ly, lz enter only through the Gaussian factor exp(-ds k^2)
+ * (init_cuda.cu:394-428), k_a = 2 pi m / L_a. */
+
+/* Change the box (unit-cell) lengths: rewrites the spectral gain tables in
+ * place.  The fields keep their grid values. */
+int scft_set_box(scft_ctx *ctx, double lx, double ly, double lz);
+/* The current box lengths (lx, ly, lz). */
+int scft_get_box(const scft_ctx *ctx, double *L3);
+
+/* SCFT stress of the propagators stored by the last getConc:
+ * dF_dL[b*3 + a] = -d ln Q_b / dL_a at fixed fields (the partial derivative
+ * of F at fixed w; at a saddle point it is the total dF/dL of the converged
+ * free energy).  Spectral contraction of q and q+ with d exp(-ds k^2)/dL. */
+int scft_stress(scft_ctx *ctx, double *dF_dL);
+
+/* Reverse-mode adjoint (vector-Jacobian product) of getConc
+ * (cuda_scft.cu:61-138) at the current fields: for the map
+ * (wA, wB, box) -> (phiA, phiB, Q) and cotangents pha_bar, phb_bar
+ * ([batch][M] host, null = 0) and Q_bar ([batch], null = 0), returns
+ * wa_bar, wb_bar ([batch][M], null = not wanted) and L_bar ([batch][3],
+ * null = skip the box terms).  The forward propagators are stored only every
+ * `checkpoint_every` contour steps (0: ceil(sqrt(NsA + dNsB))) and recomputed
+ * segment by segment during the reverse sweeps.  Includes getConc's mean
+ * subtraction of wA. */
+int scft_adjoint(scft_ctx *ctx, const double *pha_bar, const double *phb_bar,
+                 const double *Q_bar, double *wa_bar, double *wb_bar, double *L_bar,
+                 int checkpoint_every);
+
+/* Propagator slices held by scft_adjoint for a checkpoint interval (0: the
+ * default), and their bytes. */
+int scft_adjoint_checkpoints(scft_ctx *ctx, int checkpoint_every, int *slices,
+                             long long *bytes);
+
+/* Unit-cell relaxation (batch == 1): converge the fields to max|dw| < tol_w
+ * (scft_converge, at most max_inner iterations), take the stress, move the
+ * box lengths selected by axes_mask (bit 0 x, 1 y, 2 z) by a Barzilai-Borwein
+ * step on F*(L) (first step step0 * stress, at most 5% per step), and repeat
+ * until max |stress| < tol_stress or max_outer rounds.  Returns the rounds,
+ * the final stress [3] and the free energy [5] of the final fields; the box
+ * is left at the relaxed lengths. */
+int scft_relax_cell(scft_ctx *ctx, int axes_mask, double tol_w, double tol_stress,
+                    int max_outer, int max_inner, double step0, int *outer_iters,
+                    double *dF_dL, double *out5);
+
 #ifdef __cplusplus
 }
 #endif

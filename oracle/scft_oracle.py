@@ -338,6 +338,77 @@ class FreeResult:
     log: list = field(default_factory=list)   # (iter, b, F, FAB, FW, FS, incomp)
 
 
+# ------------------------------------------------------------ derivatives
+# No reference counterpart: the checks of the CUDA adjoint and stress.  The
+# box enters only through kxyzdz (init_cuda.cu:394-428), k_a = 2 pi m / L_a.
+
+def with_box(p: Params, lx=None, ly=None, lz=None) -> Params:
+    import dataclasses
+    return dataclasses.replace(p, lx=p.lx if lx is None else lx, ly=p.ly if ly is None else ly,
+                               lz=p.lz if lz is None else lz)
+
+
+def conc_functional(wa, wb, p: Params, pha_bar=None, phb_bar=None, Q_bar=None):
+    """J = sum(pha_bar*phiA) + sum(phb_bar*phiB) + sum_b Q_bar[b]*Q[b] of
+    getConc (cuda_scft.cu:61-138) at (wa, wb, box of p)."""
+    c = get_conc(wa, wb, p)
+    J = 0.0
+    if pha_bar is not None:
+        J += float((pha_bar * c.pha).sum())
+    if phb_bar is not None:
+        J += float((phb_bar * c.phb).sum())
+    if Q_bar is not None:
+        J += float((np.asarray(Q_bar) * c.Q).sum())
+    return J
+
+
+def stress_fd(wa, wb, p: Params, h_rel=1e-4):
+    """Central finite differences of -ln Q per box axis, h = h_rel * L:
+    -> [batch][3]."""
+    out = np.zeros((wa.shape[0], 3))
+    lens = (p.lx, p.ly, p.lz)
+    for a in range(3):
+        h = h_rel * lens[a]
+        Qs = []
+        for sgn in (+1, -1):
+            L = list(lens)
+            L[a] += sgn * h
+            Qs.append(get_conc(wa, wb, with_box(p, *L)).Q)
+        out[:, a] = -(np.log(Qs[0]) - np.log(Qs[1])) / (2 * h)
+    return out
+
+
+def stress_spectral(wa, wb, p: Params):
+    """Analytic SCFT stress -d ln Q/dL_a at fixed fields: sum over contour
+    steps of <q+(s), W (dK/dL_a) W q(s-1)> / (M Q), with dK/dL_a the
+    diffusion filter whose Gaussian factor is multiplied by 2 ds k_a^2/L_a.
+    -> [batch][3]."""
+    c = get_conc(wa, wb, p)
+    G = kxyzdz_half(p)
+    k2 = [k2_axis(p.nx, p.lx)[None, None, : p.nx // 2 + 1],
+          k2_axis(p.ny, p.ly)[None, :, None], k2_axis(p.nz, p.lz)[:, None, None]]
+    lens = (p.lx, p.ly, p.lz)
+    dG = [G * 2 * p.ds0 * k2[a] / lens[a] for a in range(3)]
+    axes = (1, 2, 3)
+    out = np.zeros((wa.shape[0], 3))
+    blocks = ((c.qa, c.qca, c.wa, p.NsA), (c.qb, c.qcb, wb, p.dNsB))
+    for q, qc, w, ns in blocks:
+        W = np.exp(-w * p.ds2)
+        for s in range(1, ns + 1):
+            U = np.fft.rfftn(W * q[:, s - 1], axes=axes)
+            for a in range(3):
+                t = W * np.fft.irfftn(U * dG[a][None], s=p.shape, axes=axes)
+                out[:, a] += (t * qc[:, s]).reshape(wa.shape[0], -1).sum(axis=1)
+    return -out / (p.M * c.Q[:, None])
+
+
+def free_energy_of(wa, wb, p: Params):
+    """F of Free's formula (cuda_scft.cu:190-221) with phi and Q of getConc at
+    these fields: -> [batch]."""
+    c = get_conc(wa, wb, p)
+    return free_energy(c.wa, wb, c.pha, c.phb, c.Q, p.hAB)[0]
+
+
 def free_loop(wa, wb, p: Params, max_it: int, writer=None) -> FreeResult:
     """``Free`` (cuda_scft.cu:140-269): ``max_it`` SCF iterations of
     average_value(wa), average_value(wb), getConc, phi_w; every ``AverIt``

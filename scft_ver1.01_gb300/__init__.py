@@ -40,7 +40,8 @@ EXPORTS = [
     "scft_copy_fields", "scft_group_create", "scft_group_destroy", "scft_group_last_error",
     "scft_group_iterate", "scft_group_time_iterations", "scft_group_launch_count",
     "scft_get_schedule", "scft_write_vtk", "scft_convert_pha_to_vtk", "scft_set_target",
-    "scft_phi_w_constrained",
+    "scft_phi_w_constrained", "scft_set_box", "scft_stress", "scft_adjoint",
+    "scft_adjoint_checkpoints", "scft_relax_cell", "scft_get_box",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
 FLAG_AUTOTUNE = 32
@@ -125,6 +126,14 @@ def load_library(path: str | None = None):
         "scft_convert_pha_to_vtk": (C.c_int, [C.c_char_p, C.c_char_p]),
         "scft_set_target": (C.c_int, [vp, dp]),
         "scft_phi_w_constrained": (C.c_int, [vp, C.c_int, C.c_double]),
+        "scft_set_box": (C.c_int, [vp, C.c_double, C.c_double, C.c_double]),
+        "scft_get_box": (C.c_int, [vp, dp]),
+        "scft_stress": (C.c_int, [vp, dp]),
+        "scft_adjoint": (C.c_int, [vp, dp, dp, dp, dp, dp, dp, C.c_int]),
+        "scft_adjoint_checkpoints": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int),
+                                               C.POINTER(C.c_longlong)]),
+        "scft_relax_cell": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
+                                      C.c_double, C.POINTER(C.c_int), dp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -345,6 +354,56 @@ class Context:
     def phi_w_constrained(self, ex: bool = False, lam: float = 0.0):
         """One phi_w_constrained (ex False) or phi_w_constrainedEx (ex True) update."""
         self._ck(self.lib.scft_phi_w_constrained(self.h, int(bool(ex)), lam))
+
+    def set_box(self, lx: float, ly: float, lz: float):
+        self._ck(self.lib.scft_set_box(self.h, lx, ly, lz))
+        self.params.lx, self.params.ly, self.params.lz = lx, ly, lz
+
+    def box(self) -> np.ndarray:
+        out = np.empty(3)
+        self._ck(self.lib.scft_get_box(self.h, _dptr(out)))
+        return out
+
+    def stress(self) -> np.ndarray:
+        """-d ln Q / dL [batch, 3] of the propagators of the last getConc."""
+        out = np.empty((self.shape[0], 3))
+        self._ck(self.lib.scft_stress(self.h, _dptr(out)))
+        return out
+
+    def adjoint(self, pha_bar=None, phb_bar=None, Q_bar=None, want_L: bool = True,
+                checkpoint_every: int = 0):
+        """Vector-Jacobian product of getConc at the current fields:
+        -> (wa_bar, wb_bar, L_bar[batch, 3] or None)."""
+        def seed(a):
+            if a is None:
+                return None
+            return np.ascontiguousarray(np.broadcast_to(a, self.shape), dtype=np.float64)
+        pa, pb = seed(pha_bar), seed(phb_bar)
+        qb = None if Q_bar is None else np.ascontiguousarray(
+            np.broadcast_to(Q_bar, (self.shape[0],)), dtype=np.float64)
+        wa_bar, wb_bar = np.empty(self.shape), np.empty(self.shape)
+        L_bar = np.empty((self.shape[0], 3)) if want_L else None
+        p = lambda a: None if a is None else _dptr(a)
+        self._ck(self.lib.scft_adjoint(self.h, p(pa), p(pb), p(qb), _dptr(wa_bar), _dptr(wb_bar),
+                                       p(L_bar), checkpoint_every))
+        return wa_bar, wb_bar, L_bar
+
+    def relax_cell(self, axes_mask: int = 7, tol_w: float = 1e-8, tol_stress: float = 1e-6,
+                   max_outer: int = 50, max_inner: int = 5000, step0: float = 1.0):
+        """Unit-cell relaxation -> (rounds, final stress [3], free energy [5]);
+        the context keeps the relaxed box (``box()``)."""
+        n = C.c_int()
+        sig, fe = np.empty(3), np.empty(5)
+        self._ck(self.lib.scft_relax_cell(self.h, axes_mask, tol_w, tol_stress, max_outer,
+                                          max_inner, step0, C.byref(n), _dptr(sig), _dptr(fe)))
+        return n.value, sig, fe
+
+    def adjoint_checkpoints(self, checkpoint_every: int = 0):
+        """-> (propagator slices held by the adjoint, bytes)."""
+        n, b = C.c_int(), C.c_longlong()
+        self._ck(self.lib.scft_adjoint_checkpoints(self.h, checkpoint_every, C.byref(n),
+                                                   C.byref(b)))
+        return n.value, b.value
 
 
 class Group:

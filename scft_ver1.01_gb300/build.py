@@ -23,7 +23,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 
 SOURCES = ["capi.cu", "io.cpp", "compat.cpp", "k_line.cu", "k_fields.cu", "k_fast.cu",
-           "k_anderson.cu", "group.cu", "noalloc.cu"]
+           "k_anderson.cu", "group.cu", "noalloc.cu", "adjoint.cu"]
 # Drop-in driver of the reference's struct API (init_scft -> fft_test ->
 # finalize_cufft), linked against the library: the reference's `scan` binary.
 DRIVER_SRC = "scft_main.cpp"

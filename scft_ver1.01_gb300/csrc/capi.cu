@@ -44,6 +44,54 @@ std::vector<double> k2_axis(int n, double L) {
   return k;
 }
 
+// Gains of the passes (kxyzdz, init_cuda.cu:394-428, split per axis:
+// exp(-ds0 k^2)/n, with the constant factors of length-1 axes folded into the
+// first pass) and their box derivatives: d/dL_a of exp(-ds0 k_a^2) is
+// exp(-ds0 k_a^2) * 2 ds0 k_a^2 / L_a because k_a is proportional to 1/L_a.
+// Rewritten in place when the box changes.
+int upload_gains(scft_ctx *ctx) {
+  const scft_params &p = ctx->p;
+  const int dims[3] = {p.nx, p.ny, p.nz};
+  const double lens[3] = {p.lx, p.ly, p.lz};
+  const size_t rb = ctx->rbytes;
+  double scalar = 1.0;
+  for (int a = 0; a < 3; ++a) {
+    ctx->unit_c[a] = 0.0;
+    if (dims[a] == 1) {
+      const double k2 = k2_axis(1, lens[a])[0];
+      scalar *= exp(-p.ds0 * k2);
+      ctx->unit_c[a] = 2.0 * p.ds0 * k2 / lens[a];
+    }
+  }
+  size_t dbytes = 0;
+  for (const AxisPlan &ap : ctx->passes) dbytes += ((size_t)ap.n * rb + 255) & ~(size_t)255;
+  if (!ctx->dgain) CK(cudaMalloc(&ctx->dgain, dbytes));
+  size_t doff = 0;
+  for (size_t pi = 0; pi < ctx->passes.size(); ++pi) {
+    const AxisPlan &ap = ctx->passes[pi];
+    const int a = ctx->pass_axis[pi];
+    const std::vector<double> k2 = k2_axis(ap.n, lens[a]);
+    std::vector<double> g(ap.n), dg(ap.n);
+    for (int m = 0; m < ap.n; ++m) {
+      g[m] = exp(-p.ds0 * k2[m]) / ap.n;
+      if (pi == 0) g[m] *= scalar;
+      dg[m] = g[m] * 2.0 * p.ds0 * k2[m] / lens[a];
+    }
+    void *dptr = static_cast<unsigned char *>(ctx->dgain) + doff;
+    ctx->dgain_pass[pi] = dptr;
+    doff += ((size_t)ap.n * rb + 255) & ~(size_t)255;
+    if (rb == 4) {
+      std::vector<float> gf(g.begin(), g.end()), dgf(dg.begin(), dg.end());
+      CK(cudaMemcpy(const_cast<void *>(ap.gain), gf.data(), 4 * ap.n, cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(dptr, dgf.data(), 4 * ap.n, cudaMemcpyHostToDevice));
+    } else {
+      CK(cudaMemcpy(const_cast<void *>(ap.gain), g.data(), 8 * ap.n, cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(dptr, dg.data(), 8 * ap.n, cudaMemcpyHostToDevice));
+    }
+  }
+  return SCFT_OK;
+}
+
 bool radix_plan(int n, int *fac, int *nfac) {
   int m = n, k = 0;
   while (m % 4 == 0) { fac[k++] = 4; m /= 4; }
@@ -471,7 +519,8 @@ void free_all(scft_ctx *ctx) {
   cudaFree(ctx->partial); cudaFree(ctx->sum); cudaFree(ctx->Q); cudaFree(ctx->ffl);
   cudaFree(ctx->fe5); cudaFree(ctx->tables); cudaFree(ctx->dev_err);
   cudaFree(ctx->res); cudaFree(ctx->rpartial); cudaFree(ctx->gram); cudaFree(ctx->and_a);
-  cudaFree(ctx->and_lam); cudaFree(ctx->target);
+  cudaFree(ctx->and_lam); cudaFree(ctx->target); cudaFree(ctx->dgain);
+  scft_internal_adjoint_free(ctx);
   for (double *h : ctx->hist_w) cudaFree(h);
   for (double *h : ctx->hist_d) cudaFree(h);
   ctx->hist_w.clear();
@@ -543,6 +592,47 @@ int autotune(scft_ctx *ctx) {
 // Hooks for the group graph (group.cu).
 int scft_internal_pre_mix(scft_ctx *ctx) { return pre_mix(ctx); }
 int scft_internal_mix(scft_ctx *ctx) { return mix(ctx); }
+int scft_internal_get_conc(scft_ctx *ctx) { return get_conc(ctx); }
+
+namespace {
+template <typename R>
+int filter_impl(scft_ctx *ctx, const R *in, long long in_bs, R *out, long long out_bs,
+                const R *pre, const R *post, long long w_bs, int nb, int deriv_pass, R *s0,
+                R *s1, cudaStream_t st) {
+  const long long M = ctx->M;
+  const int np = (int)ctx->passes.size();
+  for (int pi = 0; pi < np; ++pi) {
+    scft::PassSet<R> p;
+    memset(&p, 0, sizeof(p));
+    p.nset = 1;
+    p.batch = nb;
+    p.w_bs = w_bs;
+    p.in[0] = pi == 0 ? in : ((pi - 1) & 1 ? s1 : s0);
+    p.in_bs[0] = pi == 0 ? in_bs : M;
+    p.out[0] = pi == np - 1 ? out : (pi & 1 ? s1 : s0);
+    p.out_bs[0] = pi == np - 1 ? out_bs : M;
+    p.pre[0] = pi == 0 ? pre : nullptr;
+    p.post[0] = pi == np - 1 ? post : nullptr;
+    AxisPlan ap = ctx->passes[pi];
+    if (pi == deriv_pass) ap.gain = ctx->dgain_pass[pi];
+    int rc = launch_set<R>(ctx, ap, p, st);
+    if (rc) return rc;
+  }
+  return SCFT_OK;
+}
+}  // namespace
+
+int scft_internal_filter(scft_ctx *ctx, const void *in, long long in_bs, void *out,
+                         long long out_bs, const void *pre, const void *post, long long w_bs,
+                         int nb, int deriv_pass, void *s0, void *s1, cudaStream_t st) {
+  if (ctx->rbytes == 4)
+    return filter_impl<float>(ctx, (const float *)in, in_bs, (float *)out, out_bs,
+                              (const float *)pre, (const float *)post, w_bs, nb, deriv_pass,
+                              (float *)s0, (float *)s1, st);
+  return filter_impl<double>(ctx, (const double *)in, in_bs, (double *)out, out_bs,
+                             (const double *)pre, (const double *)post, w_bs, nb, deriv_pass,
+                             (double *)s0, (double *)s1, st);
+}
 
 int scft_fail(scft_ctx *ctx, int status, const std::string &msg) {
   if (ctx) ctx->err = msg;
@@ -694,12 +784,9 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   // ---- per-axis spectral tables (init_cuda.cu:394-428, split per axis)
   const int dims[3] = {p.nx, p.ny, p.nz};
   const double lens[3] = {p.lx, p.ly, p.lz};
-  double scalar = 1.0;  // gains of length-1 axes, folded into the first pass
   std::vector<int> axes;
-  for (int a = 0; a < 3; ++a) {
-    if (dims[a] == 1) scalar *= exp(-p.ds0 * k2_axis(1, lens[a])[0]);
-    else axes.push_back(a);
-  }
+  for (int a = 0; a < 3; ++a)
+    if (dims[a] != 1) axes.push_back(a);
   size_t tab_bytes = 0;
   for (int a : axes) tab_bytes += (size_t)dims[a] * 3 * rb + 256;
   if (!alloc(&ctx->tables, tab_bytes)) return fail(SCFT_ERR_NO_MEMORY, "table allocation failed");
@@ -731,28 +818,24 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     ap.use_fast = (rb == 4 && scft::fast_line_supported(ap)) ? 1 : 0;
     if (scft::line_filter_smem_bytes(ap, rb) > (size_t)scft::kLineSmemMax)
       return fail(SCFT_ERR_UNSUPPORTED, "line too long for shared memory");
-    // twiddles exp(-2 pi i m / n) and gains exp(-ds0 k^2)/n
-    const std::vector<double> k2 = k2_axis(n, lens[a]);
+    // twiddles exp(-2 pi i m / n); the gains are filled by upload_gains
     const size_t tw_off = off, g_off = off + (size_t)n * 2 * rb;
     for (int m = 0; m < n; ++m) {
       const double ang = -2.0 * M_PI * (double)m / (double)n;
       const double c = cos(ang), s = sin(ang);
-      double g = exp(-p.ds0 * k2[m]) / n;
-      if (ai == 0) g *= scalar;
       if (rb == 4) {
         float *t = reinterpret_cast<float *>(&host[tw_off]);
         t[2 * m] = (float)c; t[2 * m + 1] = (float)s;
-        reinterpret_cast<float *>(&host[g_off])[m] = (float)g;
       } else {
         double *t = reinterpret_cast<double *>(&host[tw_off]);
         t[2 * m] = c; t[2 * m + 1] = s;
-        reinterpret_cast<double *>(&host[g_off])[m] = g;
       }
     }
     ap.twiddle = static_cast<unsigned char *>(ctx->tables) + tw_off;
     ap.gain = static_cast<unsigned char *>(ctx->tables) + g_off;
     off += (size_t)n * 3 * rb;
     off = (off + 255) & ~(size_t)255;
+    ctx->pass_axis[ctx->passes.size()] = a;
     ctx->passes.push_back(ap);
   }
   // x and y both as their own passes (no length-1 axis among them) and small
@@ -762,6 +845,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
                  scft::xy_fusable(ctx->passes[0], ctx->passes[1]);
   if (cudaMemcpy(ctx->tables, host.data(), tab_bytes, cudaMemcpyHostToDevice) != cudaSuccess)
     return fail(SCFT_ERR_CUDA, "table upload failed");
+  if (upload_gains(ctx)) return fail(SCFT_ERR_CUDA, "gain table upload failed: " + ctx->err);
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(SCFT_ERR_CUDA, "set-up failed");
   ctx->err = "no error";
   if (p.flags & SCFT_FLAG_AUTOTUNE) {
@@ -943,6 +1027,28 @@ int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir) {
 int scft_synchronize(scft_ctx *ctx) {
   if (!ctx) return SCFT_ERR_INVALID_ARG;
   return sync_check(ctx);
+}
+
+int scft_set_box(scft_ctx *ctx, double lx, double ly, double lz) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  if (!(lx > 0 && ly > 0 && lz > 0)) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad box");
+  CK(cudaSetDevice(ctx->p.device));
+  // the tables are read by every pass launch (the captured graphs included,
+  // also a group's): no launch of this context may be in flight
+  CK(cudaDeviceSynchronize());
+  ctx->p.lx = lx;
+  ctx->p.ly = ly;
+  ctx->p.lz = lz;
+  ctx->and_count = 0;   // the history belongs to the old operator
+  return upload_gains(ctx);
+}
+
+int scft_get_box(const scft_ctx *ctx, double *L3) {
+  if (!ctx || !L3) return SCFT_ERR_INVALID_ARG;
+  L3[0] = ctx->p.lx;
+  L3[1] = ctx->p.ly;
+  L3[2] = ctx->p.lz;
+  return SCFT_OK;
 }
 
 int scft_get_schedule(const scft_ctx *ctx, int *flags, double *march_ms) {

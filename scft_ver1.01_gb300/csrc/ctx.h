@@ -55,6 +55,13 @@ struct scft_ctx {
   // spectral tables (twiddles + gains of each pass), device
   void *tables = nullptr;
   std::vector<scft::AxisPlan> passes;
+  int pass_axis[3] = {0, 0, 0};       // grid axis (0 x, 1 y, 2 z) of each pass
+  // box derivatives: per pass the gain times d(-ds k^2)/dL of its axis,
+  // and for length-1 axes (no pass) the constant d(-ds k^2)/dL
+  void *dgain = nullptr;
+  const void *dgain_pass[3] = {nullptr, nullptr, nullptr};
+  double unit_c[3] = {0.0, 0.0, 0.0};
+  struct AdjointState *adj = nullptr;   // adjoint / stress work buffers (lazy)
   // per-march event timing
   bool profiling = false;
   std::vector<cudaEvent_t> prof_events;   // pairs, grown on demand
@@ -64,3 +71,16 @@ struct scft_ctx {
 
 // Set ctx->err and return status.
 int scft_fail(scft_ctx *ctx, int status, const std::string &msg);
+
+// One application of the step operator's diffusion part to nb slices:
+// out = post * K (pre * in), K = the per-axis line filters of the context
+// (x, y, z passes, no plane fusion).  deriv_pass >= 0 swaps that pass's gain
+// for its box-derivative gain.  s0 and s1 hold the intermediates (nb slices
+// of M each); in, out, s0 and s1 must not overlap.  Working precision.
+int scft_internal_filter(scft_ctx *ctx, const void *in, long long in_bs, void *out,
+                         long long out_bs, const void *pre, const void *post, long long w_bs,
+                         int nb, int deriv_pass, void *s0, void *s1, cudaStream_t st);
+// getConc (cuda_scft.cu:61-138) on the context's fields.
+int scft_internal_get_conc(scft_ctx *ctx);
+// Releases the adjoint work buffers (adjoint.cu).
+void scft_internal_adjoint_free(scft_ctx *ctx);

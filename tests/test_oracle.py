@@ -184,3 +184,18 @@ def test_oracle_anderson_beats_simple_mixing(orc):
     # at the saddle point incompressibility holds and the residual vanishes
     _, _, emax, _, _, _ = orc.residual(ra[0], ra[1], ra[2], ra[3], p.hAB, p.wcmp)
     assert emax[0] < 1e-3
+
+
+def test_analytic_stress_matches_finite_differences(orc):
+    """The spectral stress formula (q, q+ contracted with d exp(-ds k^2)/dL)
+    equals central differences of -ln Q with h = 1e-4 L, including the
+    constant wave number of a length-1 axis."""
+    rng = np.random.default_rng(1)
+    for grid in ((12, 8, 6), (12, 8, 1)):
+        p = orc.Params(nx=grid[0], ny=grid[1], nz=grid[2], lx=3.1, ly=2.7, lz=2.2, hAB=15.0,
+                       fA=0.4, ds0=0.05, batch=2)
+        wa = rng.normal(0, 1.5, (2,) + p.shape)
+        wb = rng.normal(0, 1.5, (2,) + p.shape)
+        a = orc.stress_spectral(wa, wb, p)
+        b = orc.stress_fd(wa, wb, p)
+        assert np.abs(a - b).max() < 1e-7 * np.abs(a).max()
