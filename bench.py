@@ -226,6 +226,106 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
     return out
 
 
+def stress_leg(pkg, dev, relax=False, budget_s=60.0):
+    """Config 3: hexagonal cylinders, f=0.3, chiN=25, 128x128x64, box
+    Lx=4.2, Ly=Lx*sqrt(3), Lz=2.0, Ns=200, FP32 propagation with FP64
+    reductions, Anderson m=20.  Converges the fields (FP32 floor 3e-5), then
+    times the box stress (-d ln Q/dL from the stored propagators) and the
+    checkpointed adjoint; checks the stress against an FP64 context and
+    against central differences of FP64 ln Q with h = 1e-4 L.  With relax,
+    also runs the stress-driven unit-cell relaxation of Lx, Ly."""
+    import math
+    from scft_gb300 import fields as fl
+    nx, ny, nz, lx, lz = 128, 128, 64, 4.2, 2.0
+    ly = lx * math.sqrt(3)
+    kw = dict(nx=nx, ny=ny, nz=nz, lx=lx, ly=ly, lz=lz, hAB=25.0, fA=0.3, ds0=0.005,
+              mixing=pkg.MIX_ANDERSON, anderson_history=20, device=dev)
+    wa, wb = fl.hexagonal(nx, ny, nz, lx, ly, lz, 25.0, seed=0)
+    out = {"config": "128x128x64 hexagonal cylinders, f=0.3, chiN=25, box 4.2 x 7.2746 x 2.0, "
+                     "Ns=200, FP32 propagation, Anderson m=20"}
+    with pkg.Context(precision=pkg.PREC_FP32, **kw) as c:
+        c.set_w(wa, wb)
+        t0 = time.perf_counter()
+        it, fe, ok = converge_timed(c, 3e-5, 3000, budget_s)
+        out["converge"] = {"seconds": time.perf_counter() - t0, "iterations": it,
+                           "residual": float(c.residual()[0][0]), "F": fe[0, 0]}
+        wa1, wb1 = c.wa, c.wb
+        c.get_conc()
+        c.stress()                                   # allocation, warm-up
+        c.synchronize()
+        t0 = time.perf_counter()
+        s32 = c.stress()
+        out["stress_fp32"] = {"dF_dL": s32[0].tolist(), "ms": (time.perf_counter() - t0) * 1e3}
+        c.adjoint(None, None, 1.0)                   # allocation, warm-up
+        for want_L in (True, False):
+            t0 = time.perf_counter()
+            c.adjoint(None, None, 1.0, want_L=want_L)
+            out["adjoint_ms" + ("_with_box" if want_L else "_fields_only")] = \
+                (time.perf_counter() - t0) * 1e3
+        n_sl, by = c.adjoint_checkpoints(0)
+        out["adjoint_memory"] = {"slices": n_sl, "bytes": by,
+                                 "stored_propagators_bytes": 4 * (c.NsA + c.dNsB + 2) * nx * ny
+                                 * nz * 4}
+        out["sweep_ms_per_scf_iteration"] = c.time_iterations(3) / 3
+    with pkg.Context(precision=pkg.PREC_FP64, **kw) as c:
+        c.set_w(wa1, wb1)
+        c.get_conc()
+        s64 = c.stress()
+        fd = []
+        for a in range(3):
+            L = [lx, ly, lz]
+            h = 1e-4 * L[a]
+            lnq = []
+            for sg in (1, -1):
+                Lp = list(L)
+                Lp[a] += sg * h
+                c.set_box(*Lp)
+                c.set_w(wa1, wb1)
+                c.get_conc()
+                lnq.append(math.log(c.Q()[0]))
+            fd.append(-(lnq[0] - lnq[1]) / (2 * h))
+        den = max(abs(v) for v in fd)
+        out["stress_fp64"] = s64[0].tolist()
+        out["stress_fd_fp64_h1e-4L"] = fd
+        out["rel_err_fp64_vs_fd"] = max(abs(a - b) for a, b in zip(s64[0], fd)) / den
+        out["rel_err_fp32_vs_fp64"] = max(abs(a - b) for a, b in zip(s32[0], s64[0])) / den
+    if relax:
+        with pkg.Context(precision=pkg.PREC_FP32, **kw) as c:
+            c.set_w(wa1, wb1)
+            t0 = time.perf_counter()
+            rounds, sig, fe = c.relax_cell(axes_mask=3, tol_w=3e-5, tol_stress=1e-5,
+                                           max_outer=40, max_inner=2000)
+            out["relax"] = {"seconds": time.perf_counter() - t0, "rounds": rounds,
+                            "dF_dL": sig.tolist(), "F": fe[0], "box": c.box().tolist()}
+    return out
+
+
+def cufft_leg(dev, n=N, steps=50):
+    """cuFFT comparison (timed only as a comparison, not used by the library):
+    the same FP32 split step q <- W*irfftn(G*rfftn(W*q)) with torch.fft
+    (cuFFT R2C/C2R) at n^3, one propagator, CUDA events on torch's stream."""
+    import torch
+    d = torch.device(f"cuda:{dev}")
+    g = torch.Generator(device=d).manual_seed(0)
+    W = 1.0 + 0.01 * torch.rand((n, n, n), device=d, generator=g)
+    k = torch.fft.fftfreq(n, d=1.0 / n, device=d) * (2 * np.pi / L)
+    kr = torch.fft.rfftfreq(n, d=1.0 / n, device=d) * (2 * np.pi / L)
+    G = torch.exp(-DS * (k[:, None, None] ** 2 + k[None, :, None] ** 2 + kr[None, None, :] ** 2))
+    q = torch.ones((n, n, n), device=d)
+    for _ in range(5):
+        q = W * torch.fft.irfftn(G * torch.fft.rfftn(W * q), s=(n, n, n))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(d)
+    e0.record()
+    for _ in range(steps):
+        q = W * torch.fft.irfftn(G * torch.fft.rfftn(W * q), s=(n, n, n))
+    e1.record()
+    torch.cuda.synchronize(d)
+    ms = e0.elapsed_time(e1) / steps
+    return {"what": "torch.fft (cuFFT) FP32 split step, one propagator, %d^3" % n,
+            "us_per_step": ms * 1e3, "gpt_step_per_s": n ** 3 / (ms / 1e3) / 1e9}
+
+
 def batch_sweep_leg(pkg, dev, n_inst=64, iters=3, seed=4):
     """Config-4 phase-diagram sweep: 64 independent instances, grids drawn from
     {32^3, 48^3, 64^3}, chiN~U[12,30], f~U[0.25,0.5], box~U[3,5] Rg,
@@ -393,6 +493,10 @@ def run_ours(args):
                          else None),
             "batch_sweep": (batch_sweep_leg(pkg, dev) if (not args.no_sweep and ws == 1)
                             else None),
+            "stress_adjoint": (stress_leg(pkg, dev, relax=args.relax)
+                               if (not args.no_stress and ws == 1) else None),
+            "cufft_comparison": (cufft_leg(dev) if (headline and ws == 1 and not args.no_cufft)
+                                 else None),
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -416,6 +520,11 @@ def main():
                     help="skip the 64-instance heterogeneous sweep leg")
     ap.add_argument("--no-converge", action="store_true",
                     help="skip the seconds-to-converge leg (FP64 vs FP32+FP64 polish)")
+    ap.add_argument("--no-stress", action="store_true",
+                    help="skip the config-3 stress / adjoint leg")
+    ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT comparison leg")
+    ap.add_argument("--relax", action="store_true",
+                    help="add the unit-cell relaxation to the stress leg (minutes)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -618,17 +618,27 @@ int scft_relax_cell(scft_ctx *ctx, int axes_mask, double tol_w, double tol_stres
   double L[3] = {ctx->p.lx, ctx->p.ly, ctx->p.lz}, sig[3], fe[5];
   double L_prev[3] = {0, 0, 0}, sig_prev[3] = {0, 0, 0};
   double alpha = step0;
+  // Inexact inner solves: far from the stress-free box the fields need not be
+  // converged tightly, so each round converges to max(tol_w, stress/10) of
+  // the previous round (at most 1e-3); the last round always reaches tol_w.
+  double tol = std::max(tol_w, 1e-3);
   int it = 0;
   for (;;) {
     int iters = 0;
-    RC(scft_converge(ctx, tol_w, max_inner, &iters, fe));
+    RC(scft_converge(ctx, tol, max_inner, &iters, fe));
     RC(scft_internal_get_conc(ctx));   // propagators of the converged fields
     RC(scft_stress(ctx, sig));
     double smax = 0.0;
     for (int a = 0; a < 3; ++a)
       if (axes_mask >> a & 1) smax = std::max(smax, fabs(sig[a]));
     ++it;
-    if (smax < tol_stress || it >= max_outer) break;
+    if (it >= max_outer) break;
+    if (smax < tol_stress) {
+      if (tol <= tol_w) break;
+      tol = tol_w;   // stress-free at a loose tolerance: tighten, same box
+      continue;
+    }
+    tol = std::max(tol_w, std::min(1e-3, 0.1 * smax));
     // Barzilai-Borwein step on F*(L), whose gradient is the stress
     if (it > 1) {
       double ss = 0.0, sy = 0.0;
