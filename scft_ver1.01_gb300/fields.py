@@ -37,14 +37,16 @@ def gyroid(nx, ny, nz, lx, ly, lz, chiN, seed, batch=1, amp=0.2, noise=0.02):
 
 
 def hexagonal(nx, ny, nz, lx, ly, lz, chiN, seed, batch=1, amp=0.2, noise=0.02):
-    """Cylinders along z on a hexagonal lattice in the rectangular cell
-    Lx = a, Ly = a*sqrt(3) (two cylinders per cell): the three shortest
-    reciprocal vectors (0, 2)*2pi/L and (1, +-1)*2pi/L of that cell."""
+    """A-rich cylinders along z on a hexagonal lattice in the rectangular cell
+    Lx = a, Ly = a*sqrt(3) (two cylinders per cell, at (0, 0) and
+    (a/2, Ly/2)): h sums the three shortest reciprocal vectors (0, 2)*2pi/L
+    and (1, +-1)*2pi/L of that cell, and wA is lowest (A richest) at its
+    maxima."""
     rng = np.random.default_rng(seed)
     x, y, _ = _coords(nx, ny, nz, lx, ly, lz)
     X, Y = 2 * np.pi * x / lx, 2 * np.pi * y / ly
     h = (np.cos(2 * Y) + np.cos(X + Y) + np.cos(X - Y)) / 3.0
-    base = chiN * amp * h
+    base = -chiN * amp * h
     wa = base[None] + rng.normal(0.0, noise, (batch, nz, ny, nx))
     wb = -base[None] + rng.normal(0.0, noise, (batch, nz, ny, nx))
     return wa, wb

@@ -224,3 +224,23 @@ def test_relax_cell_lamellae(pkg):
     Fp, _ = converged_F(pkg, nx, L * 1.01, w)
     Fm, _ = converged_F(pkg, nx, L * 0.99, w)
     assert fe[0] < Fp and fe[0] < Fm
+
+
+def test_relax_cell_recovers_hexagonal_ratio(pkg):
+    """Hexagonal cylinders (f=0.3, chiN=25) in the rectangular two-cylinder
+    cell, started at a = 4.2 with Ly = a*sqrt(3): relaxing Lx and Ly
+    independently must keep Ly/Lx = sqrt(3) (the symmetry is not imposed)
+    and find a stress-free a."""
+    import math
+    from scft_gb300 import fields as fl
+    nx, ny, nz, a0 = 64, 112, 1, 4.2
+    w = fl.hexagonal(nx, ny, nz, a0, a0 * math.sqrt(3), 2.0, 25.0, seed=0)
+    with pkg.Context(nx=nx, ny=ny, nz=nz, lx=a0, ly=a0 * math.sqrt(3), lz=2.0, hAB=25.0, fA=0.3,
+                     ds0=0.01, mixing=pkg.MIX_ANDERSON, anderson_history=20) as c:
+        c.set_w(*w)
+        rounds, sig, fe = c.relax_cell(axes_mask=3, tol_w=1e-8, tol_stress=1e-6, max_outer=40,
+                                       max_inner=5000)
+        L = c.box()
+    assert rounds < 40 and max(abs(sig[0]), abs(sig[1])) < 1e-6
+    assert abs(L[1] / L[0] - math.sqrt(3)) < 1e-4
+    assert 4.3 < L[0] < 4.6
