@@ -46,6 +46,16 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, dist, device):
+    """The largest x over all ranks (the job's time is its slowest rank's)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -300,6 +310,43 @@ def stress_leg(pkg, dev, relax=False, budget_s=60.0):
     return out
 
 
+def large_leg(pkg, dev, converge=False, budget_s=120.0):
+    """Config 5: one 256^3 solve, lamellar/gyroid mixture init, f=0.45,
+    chiN=22, box 8.0 Rg, Ns=400, FP32 propagation with FP64 Q and Anderson
+    (history 30).  Throughput of 3 SCF iterations (device events) with the
+    march phase's roofline; with converge, the time to the FP32 floor."""
+    from scft_gb300 import fields as fl
+    n, Lb = 256, 8.0
+    wa, wb = fl.mixture(n, n, n, Lb, Lb, Lb, 22.0, seed=0)
+    peak, peak_kind = load_peaks()
+    with pkg.Context(nx=n, ny=n, nz=n, lx=Lb, ly=Lb, lz=Lb, hAB=22.0, fA=0.45, ds0=1.0 / 400,
+                     precision=pkg.PREC_FP32, mixing=pkg.MIX_ANDERSON, anderson_history=30,
+                     device=dev) as c:
+        c.set_w(wa, wb)
+        c.iterate(2)
+        c.synchronize()
+        c.profile_enable(16)
+        ms = c.time_iterations(3) / 3
+        march_ms, n_m, march_pts = c.profile_read()
+        c.profile_enable(0)
+        pts = 2 * (c.NsA + c.dNsB) * n ** 3
+        sched, _ = c.schedule()
+        out = {"config": "256^3 lamellar/gyroid mixture, f=0.45, chiN=22, box 8.0 Rg, Ns=400 "
+                         "(NsA=180, dNsB=220), FP32 propagation, Anderson m=30",
+               "ms_per_scf_iteration": ms, "gpt_step_per_s": pts / (ms / 1e3) / 1e9,
+               "march_roofline_frac": march_pts / (march_ms / 1e3) * 12.0 / 1e9 / peak,
+               "peak_kind": peak_kind, "schedule_flags": sched,
+               "propagator_bytes": 4 * (2 * c.NsA + 2 * c.dNsB + 4) * n ** 3}
+        if converge:
+            c.set_w(wa, wb)
+            t0 = time.perf_counter()
+            it, fe, ok = converge_timed(c, 5e-5, 5000, budget_s)
+            out["converge_to_5e-5"] = {"seconds": time.perf_counter() - t0, "iterations": it,
+                                       "converged": ok, "residual": float(c.residual()[0][0]),
+                                       "F": fe[0, 0]}
+    return out
+
+
 def cufft_leg(dev, n=N, steps=50):
     """cuFFT comparison (timed only as a comparison, not used by the library):
     the same FP32 split step q <- W*irfftn(G*rfftn(W*q)) with torch.fft
@@ -417,11 +464,7 @@ def run_ours(args):
     launches = ctx.launch_count() - l0
     barrier()
     clk = clocks.stop() if clocks else None
-    t_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(ms, dist, f"cuda:{dev}")
     value = ws * pt_steps * args.steps / (t_max / 1e3) / 1e9
 
     # ---- end-to-end through the C ABI with pinned host buffers
@@ -444,11 +487,7 @@ def run_ours(args):
             ctx._ck(ctx.lib.scft_get_field(ctx.h, pkg.FIELD_PHA, dptr(ho_a)))
             ctx._ck(ctx.lib.scft_get_field(ctx.h, pkg.FIELD_PHB, dptr(ho_b)))
         barrier()
-        e2e_s = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([e2e_s], device=f"cuda:{dev}", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{dev}")
         e2e = {"value": ws * pt_steps * e2e_steps / e2e_s / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": 2 * 8 * n ** 3, "d2h_bytes_per_step": 2 * 8 * n ** 3 + 5 * 8,
                "steps": e2e_steps,
@@ -497,6 +536,8 @@ def run_ours(args):
                                if (not args.no_stress and ws == 1) else None),
             "cufft_comparison": (cufft_leg(dev) if (headline and ws == 1 and not args.no_cufft)
                                  else None),
+            "large_256": (large_leg(pkg, dev, converge=args.large_converge)
+                          if (headline and ws == 1 and not args.no_large) else None),
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -523,6 +564,9 @@ def main():
     ap.add_argument("--no-stress", action="store_true",
                     help="skip the config-3 stress / adjoint leg")
     ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT comparison leg")
+    ap.add_argument("--no-large", action="store_true", help="skip the 256^3 Ns=400 leg")
+    ap.add_argument("--large-converge", action="store_true",
+                    help="add the 256^3 convergence run to the large leg (minutes)")
     ap.add_argument("--relax", action="store_true",
                     help="add the unit-cell relaxation to the stress leg (minutes)")
     args = ap.parse_args()

@@ -119,6 +119,14 @@ int scft_set_field(scft_ctx *ctx, int field, const double *src);
 /* Device -> host copy of one field; dst holds batch*M doubles. */
 int scft_get_field(scft_ctx *ctx, int field, double *dst);
 
+/* Zero-copy access (no reference counterpart; the reference hands out its
+ * per-GPU device pointers through CUFFT_INFO, struct.h:94-121): the device
+ * address of a field ([batch][M] FP64 on the context's device), valid until
+ * scft_destroy, and the context's CUDA stream (a cudaStream_t).  Work a
+ * caller does on the field must be ordered with that stream. */
+int scft_field_device_ptr(scft_ctx *ctx, int field, double **dptr);
+int scft_get_stream(scft_ctx *ctx, void **stream);
+
 /* average_value (cuda_scft.cu:14-59): w -= <w> per instance, on
  * SCFT_FIELD_WA or SCFT_FIELD_WB. */
 int scft_average_value(scft_ctx *ctx, int field);

@@ -41,7 +41,8 @@ EXPORTS = [
     "scft_group_iterate", "scft_group_time_iterations", "scft_group_launch_count",
     "scft_get_schedule", "scft_write_vtk", "scft_convert_pha_to_vtk", "scft_set_target",
     "scft_phi_w_constrained", "scft_set_box", "scft_stress", "scft_adjoint",
-    "scft_adjoint_checkpoints", "scft_relax_cell", "scft_get_box",
+    "scft_adjoint_checkpoints", "scft_relax_cell", "scft_get_box", "scft_field_device_ptr",
+    "scft_get_stream",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
 FLAG_AUTOTUNE = 32
@@ -128,6 +129,8 @@ def load_library(path: str | None = None):
         "scft_phi_w_constrained": (C.c_int, [vp, C.c_int, C.c_double]),
         "scft_set_box": (C.c_int, [vp, C.c_double, C.c_double, C.c_double]),
         "scft_get_box": (C.c_int, [vp, dp]),
+        "scft_field_device_ptr": (C.c_int, [vp, C.c_int, C.POINTER(dp)]),
+        "scft_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
         "scft_stress": (C.c_int, [vp, dp]),
         "scft_adjoint": (C.c_int, [vp, dp, dp, dp, dp, dp, dp, C.c_int]),
         "scft_adjoint_checkpoints": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int),
@@ -358,6 +361,20 @@ class Context:
     def set_box(self, lx: float, ly: float, lz: float):
         self._ck(self.lib.scft_set_box(self.h, lx, ly, lz))
         self.params.lx, self.params.ly, self.params.lz = lx, ly, lz
+
+    def field_view(self, field: int):
+        """A torch tensor over the device memory of a field (no copy),
+        shape [batch, Nz, Ny, Nx], float64.  Synchronise (``synchronize()`` /
+        ``torch.cuda.synchronize()``) between library calls and torch work."""
+        import torch
+        dp_out = C.POINTER(C.c_double)()
+        self._ck(self.lib.scft_field_device_ptr(self.h, field, C.byref(dp_out)))
+        addr = C.cast(dp_out, C.c_void_p).value
+
+        class _Iface:
+            __cuda_array_interface__ = {"shape": tuple(self.shape), "typestr": "<f8",
+                                        "data": (addr, False), "version": 3, "strides": None}
+        return torch.as_tensor(_Iface(), device=f"cuda:{self.params.device}")
 
     def box(self) -> np.ndarray:
         out = np.empty(3)

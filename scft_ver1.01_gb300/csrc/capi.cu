@@ -1043,6 +1043,20 @@ int scft_set_box(scft_ctx *ctx, double lx, double ly, double lz) {
   return upload_gains(ctx);
 }
 
+int scft_field_device_ptr(scft_ctx *ctx, int field, double **dptr) {
+  if (!ctx || !dptr) return SCFT_ERR_INVALID_ARG;
+  double *p = field_ptr(ctx, field);
+  if (!p) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad field");
+  *dptr = p;
+  return SCFT_OK;
+}
+
+int scft_get_stream(scft_ctx *ctx, void **stream) {
+  if (!ctx || !stream) return SCFT_ERR_INVALID_ARG;
+  *stream = ctx->st;
+  return SCFT_OK;
+}
+
 int scft_get_box(const scft_ctx *ctx, double *L3) {
   if (!ctx || !L3) return SCFT_ERR_INVALID_ARG;
   L3[0] = ctx->p.lx;

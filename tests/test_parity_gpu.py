@@ -24,6 +24,7 @@ GRIDS = [
     (128, 64, 32, 4.2, 7.3, 2.0),
     (64, 64, 1, 4.0, 4.0, 2.0),
     (256, 64, 8, 8.0, 3.0, 2.0),      # x, y fast; z (N=8) generic
+    (106, 106, 1, 21.2, 21.2, 2.0),   # the reference's out.vtk grid: radix 53, spacing 0.2
 ]
 
 
@@ -223,3 +224,19 @@ def test_error_paths(pkg):
         ctx.set_w(np.zeros(ctx.shape), np.zeros(ctx.shape))
         ctx.get_conc()
         assert abs(ctx.Q()[0] - 1) < 1e-12
+
+
+def test_field_view_is_zero_copy(pkg):
+    torch = pytest.importorskip("torch")
+    g = (16, 12, 8, 4.0, 3.0, 2.5)
+    rng = np.random.default_rng(0)
+    wa = rng.normal(0, 1, (2, 8, 12, 16))
+    with make_ctx(pkg, g, 0) as ctx:
+        ctx.set_field(pkg.FIELD_WA, wa)
+        ctx.synchronize()
+        v = ctx.field_view(pkg.FIELD_WA)
+        assert v.shape == (2, 8, 12, 16) and v.dtype == torch.float64 and v.is_cuda
+        assert np.array_equal(v.cpu().numpy(), wa)
+        v.mul_(2.0)
+        torch.cuda.synchronize()
+        assert np.array_equal(ctx.wa, 2.0 * wa)
