@@ -243,8 +243,9 @@ long long scft_group_launch_count(const scft_group *g);
  * graph, or loops that cannot afford cudaMalloc's implicit synchronisation.
  * One FP32 split step q_out = W . IFFT[G . FFT[W . q_in]] / M (one contour
  * step of sovDifFft, cuda_scft.cu:467-491) for `batch` instances laid out
- * [batch][Nz][Ny][Nx]; q_in, W and q_out are caller-owned device buffers of
- * batch*Nx*Ny*Nz floats (W: the Boltzmann factor exp(-w*ds0/2)), enqueued on
+ * [batch][Nz][Ny][Nx]; q_in, W and q_out are caller-owned, 16-byte aligned
+ * device buffers of batch*Nx*Ny*Nz floats (W: the Boltzmann factor
+ * exp(-w*ds0/2)), enqueued on
  * `stream` (a cudaStream_t; NULL = default stream).  Scratch lives in a static
  * device array of this library: batch*Nx*Ny*Nz is limited to 2^21 points
  * (larger requests return SCFT_ERR_INVALID_ARG), every GPU that loads the

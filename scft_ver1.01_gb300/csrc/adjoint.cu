@@ -590,6 +590,9 @@ int scft_adjoint_checkpoints(scft_ctx *ctx, int checkpoint_every, int *slices,
 
 int scft_stress(scft_ctx *ctx, double *dF_dL) {
   if (!ctx || !dF_dL) return SCFT_ERR_INVALID_ARG;
+  if (!ctx->have_conc)
+    return scft_fail(ctx, SCFT_ERR_INVALID_ARG,
+                     "no getConc at the current box: call scft_get_conc first");
   CK(cudaSetDevice(ctx->p.device));
   if (!ctx->adj) ctx->adj = new AdjointState();
   AdjointState &A = *ctx->adj;

@@ -403,7 +403,9 @@ int get_conc(scft_ctx *ctx) {
   if ((rc = prof_begin(ctx))) return rc;
   if ((rc = march_phase_graph(ctx))) return rc;                                // :77-112
   if ((rc = prof_end(ctx, 2.0 * (ctx->NsA + ctx->dNsB) * ctx->M * ctx->batch))) return rc;
-  return ctx->rbytes == 4 ? q_and_phi<float>(ctx) : q_and_phi<double>(ctx);
+  rc = ctx->rbytes == 4 ? q_and_phi<float>(ctx) : q_and_phi<double>(ctx);
+  ctx->have_conc = rc == SCFT_OK;
+  return rc;
 }
 
 // The field update.  Simple mixing is phi_w (cuda_aid.cu:382-416) with its
@@ -1040,6 +1042,7 @@ int scft_set_box(scft_ctx *ctx, double lx, double ly, double lz) {
   ctx->p.ly = ly;
   ctx->p.lz = lz;
   ctx->and_count = 0;   // the history belongs to the old operator
+  ctx->have_conc = false;   // the stored propagators belong to the old box
   return upload_gains(ctx);
 }
 

@@ -62,6 +62,7 @@ struct scft_ctx {
   const void *dgain_pass[3] = {nullptr, nullptr, nullptr};
   double unit_c[3] = {0.0, 0.0, 0.0};
   struct AdjointState *adj = nullptr;   // adjoint / stress work buffers (lazy)
+  bool have_conc = false;       // propagators, W and Q of a getConc at the current box
   // per-march event timing
   bool profiling = false;
   std::vector<cudaEvent_t> prof_events;   // pairs, grown on demand

@@ -31,6 +31,16 @@ template <int N, bool XP> __host__ __device__ constexpr size_t fast_core_smem() 
              : (((size_t)64 * (N + 1) * 4 + 15) / 16) * 16;
 }
 
+// Column passes keep the Boltzmann-factor tile of their output (N rows x 64
+// floats) in shared memory after the twiddle/gain tables.
+template <int N, bool XP> __host__ __device__ constexpr size_t fast_wtile_off() {
+  return ((fast_core_smem<N, XP>() + (size_t)N * 12 + 15) / 16) * 16;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
 template <int N, int P, bool XP>
 __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float> ps) {
   constexpr int R1 = N / P;
@@ -56,6 +66,25 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float
   for (int i = threadIdx.x; i < N; i += NT) {
     s_tw[i] = __ldg(reinterpret_cast<const float2 *>(ap.twiddle) + i);
     s_g[i] = __ldg(reinterpret_cast<const float *>(ap.gain) + i);
+  }
+  // Column passes with a post factor: the factor's tile does not depend on
+  // the previous pass either, so its cp.async copies are issued here too and
+  // land while the lines are loaded and filtered (the epilogue then reads
+  // shared memory instead of waiting on global loads).
+  float *s_wt = reinterpret_cast<float *>(smem_raw + fast_wtile_off<N, XP>());
+  if constexpr (!XP) {
+    if (post) {
+      const float *wt = post + b * w_bs + (long long)blockIdx.y * ap.s_outer +
+                        (long long)blockIdx.x * 64;
+      for (int c = threadIdx.x; c < N * 16; c += NT) {
+        const int row = c >> 4, part = c & 15;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                         smem_addr(s_wt + row * 64 + part * 4)),
+                     "l"(wt + (long long)row * ap.s_n + part * 4)
+                     : "memory");
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    }
   }
   // the input slice is the previous pass's output
   pdl_wait();
@@ -166,13 +195,16 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float
     }
   } else {
     float *dst = out + b * out_bs + base;
-    const float *wdst = post ? post + b * w_bs + base : nullptr;
+    if (post) {
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      __syncthreads();   // every thread's tile copies are visible
+    }
     reg::static_for<0, R1>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
       const long long off = (long long)(p + P * j) * ap.s_n;
       float2 r = v[j];
-      if (wdst) {
-        const float2 w = __ldg(reinterpret_cast<const float2 *>(wdst + off));
+      if (post) {
+        const float2 w = reinterpret_cast<const float2 *>(s_wt)[(p + P * j) * 32 + lane];
         r.x *= w.x;
         r.y *= w.y;
       }
@@ -438,16 +470,21 @@ __global__ void __launch_bounds__(256 * G, G == 1 ? 2 : 1)
     twy[i] = __ldg(reinterpret_cast<const float2 *>(apy.twiddle) + i);
     gy[i] = __ldg(reinterpret_cast<const float *>(apy.gain) + i);
   }
+  // The Boltzmann factor does not depend on the previous pass: its loads are
+  // issued before the dependency wait and overlap that pass's tail.  Then
+  // every load of the plane is in flight at once (NX*NY/NT per thread):
+  // +4% at 128^3 over 8 in flight, measured; staging through cp.async was
+  // slower.
+  constexpr int PER = NX * NY / NT;
+  float wr[PER];
+#pragma unroll
+  for (int k = 0; k < PER; ++k) wr[k] = pre ? __ldg(pre + threadIdx.x + k * NT) : 1.0f;
   pdl_wait();   // the plane is the previous pass's output
   pdl_release();
-  // every load of the plane in flight at once (NX*NY/NT of q and of W per
-  // thread): +4% at 128^3 over 8 in flight, measured; staging through
-  // cp.async was slower
 #pragma unroll
-  for (int i = threadIdx.x; i < NX * NY; i += NT) {
-    float x = __ldg(in + i);
-    if (pre) x *= __ldg(pre + i);
-    plane[(i / NX) * PITCH + (i % NX)] = x;
+  for (int k = 0; k < PER; ++k) {
+    const int i = threadIdx.x + k * NT;
+    plane[(i / NX) * PITCH + (i % NX)] = __ldg(in + i) * wr[k];
   }
   __syncthreads();
   // x pass, NY/64 rounds of 32 complex rows
@@ -495,7 +532,8 @@ __global__ void __launch_bounds__(256 * G, G == 1 ? 2 : 1)
 }
 
 template <int N, int P, bool XP> size_t fast_smem() {
-  return fast_core_smem<N, XP>() + (size_t)N * (sizeof(float2) + sizeof(float));
+  return XP ? fast_core_smem<N, XP>() + (size_t)N * (sizeof(float2) + sizeof(float))
+            : fast_wtile_off<N, XP>() + (size_t)N * 64 * sizeof(float);
 }
 
 template <int N, int P, bool XP>
@@ -606,6 +644,12 @@ cudaError_t fast_line_prepare() {
 
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
   if (ps.nset < 1 || ps.nset > kMaxSet) return cudaErrorInvalidValue;
+  // column passes copy their post-factor tile with 16-byte cp.async and move
+  // lines as float2: refuse misaligned buffers instead of faulting
+  for (int k = 0; k < ps.nset; ++k)
+    if ((reinterpret_cast<uintptr_t>(ps.post[k]) | reinterpret_cast<uintptr_t>(ps.pre[k]) |
+         reinterpret_cast<uintptr_t>(ps.in[k]) | reinterpret_cast<uintptr_t>(ps.out[k])) & 15)
+      return cudaErrorMisalignedAddress;
   const bool xp = ap.n_fast != 0;
   // column passes: the persistent pipelined kernel when the caller supplied
   // an error word for its bounded waits

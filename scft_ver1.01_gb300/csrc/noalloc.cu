@@ -81,6 +81,9 @@ extern "C" int scft_split_step_noalloc(int nx, int ny, int nz, double lx, double
                                        double ds0, int batch, const float *q_in, const float *W,
                                        float *q_out, void *stream) {
   if (!q_in || !W || !q_out) return fail(SCFT_ERR_INVALID_ARG, "null buffer");
+  if ((reinterpret_cast<uintptr_t>(q_in) | reinterpret_cast<uintptr_t>(W) |
+       reinterpret_cast<uintptr_t>(q_out)) & 15)
+    return fail(SCFT_ERR_INVALID_ARG, "q_in, W and q_out must be 16-byte aligned");
   if (batch < 1 || !(lx > 0 && ly > 0 && lz > 0 && ds0 > 0))
     return fail(SCFT_ERR_INVALID_ARG, "bad batch, box or ds0");
   if (!scft_grid_supported(nx, ny, nz) || nx > kNoAllocMaxAxis || ny > kNoAllocMaxAxis ||

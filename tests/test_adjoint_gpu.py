@@ -244,3 +244,16 @@ def test_relax_cell_recovers_hexagonal_ratio(pkg):
     assert rounds < 40 and max(abs(sig[0]), abs(sig[1])) < 1e-6
     assert abs(L[1] / L[0] - math.sqrt(3)) < 1e-4
     assert 4.3 < L[0] < 4.6
+
+
+def test_stress_needs_a_get_conc_at_the_current_box(pkg, orc):
+    ctx, p = make(pkg, orc, CASES[0], batch=1)
+    with ctx:
+        with pytest.raises(pkg.ScftError):
+            ctx.stress()
+        ctx.set_w(*fields(p.shape, 1, 1))
+        ctx.get_conc()
+        ctx.stress()
+        ctx.set_box(3.0, 2.0, 2.0)
+        with pytest.raises(pkg.ScftError):
+            ctx.stress()
