@@ -88,6 +88,8 @@ typedef struct scft_params {
 #define SCFT_FLAG_LOCKSTEP 8      /* march chains in shared lockstep launches (default below 2^20 points) */
 #define SCFT_FLAG_NO_XY 16        /* separate x and y passes instead of the fused plane kernel */
 #define SCFT_FLAG_AUTOTUNE 32     /* time every legal schedule at creation and keep the fastest */
+#define SCFT_FLAG_NO_FUSED_STEPS 64 /* two-stream chains: two launches per contour step instead of
+                                       one fused kernel per step pair (k_zz / k_xyxy) */
 
 /* Fill *p with the reference defaults (32^3, box 4, xN 20, fa 0.5,
  * ds0 0.01, batch 1, FP64, simple mixing wopt 0.05 wcmp 0.10). */

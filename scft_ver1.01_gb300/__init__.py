@@ -45,7 +45,7 @@ EXPORTS = [
     "scft_get_stream",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
-FLAG_AUTOTUNE = 32
+FLAG_AUTOTUNE, FLAG_NO_FUSED_STEPS = 32, 64
 
 
 class ScftParams(C.Structure):

@@ -21,6 +21,7 @@ struct scft_ctx {
   bool use_pipe = false;        // persistent pipelined column passes (opt-in)
   bool two_streams = false;     // march chains on two forked streams instead of lockstep
   bool fuse_xy = false;         // x and y passes fused into one plane kernel (FP32)
+  bool fuse_steps = false;      // two-stream chains run fused step pairs (one launch per step)
   double tuned_ms = 0.0;        // march-phase time of the autotuned schedule
   cudaStream_t st2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;

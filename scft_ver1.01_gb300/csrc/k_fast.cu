@@ -531,6 +531,197 @@ __global__ void __launch_bounds__(256 * G, G == 1 ? 2 : 1)
   }
 }
 
+// ------------------------------------------------------------------------
+// Fused step pair on column lines (lines along z, or y when z is absent):
+// finishes step s with the line filter and the post factor (stored to qout)
+// and starts step s+1 with the factor again and the filter (stored to out).
+// Geometry, tables and the cp.async factor tile as in the column branch of
+// k_fast_line.
+template <int N, int P>
+__global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<float> ps) {
+  constexpr int R1 = N / P;
+  constexpr int NT = P * 32;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float2 *ex = reinterpret_cast<float2 *>(smem_raw);
+  const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
+  const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
+  const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
+  const float *__restrict__ in = ps.in[set];
+  float *__restrict__ out = ps.out[set];
+  float *__restrict__ qo = ps.qout[set];
+  const float *__restrict__ w = ps.post[set];
+  float2 *s_tw = reinterpret_cast<float2 *>(smem_raw + fast_core_smem<N, false>());
+  float *s_g = reinterpret_cast<float *>(s_tw + N);
+  for (int i = threadIdx.x; i < N; i += NT) {
+    s_tw[i] = __ldg(reinterpret_cast<const float2 *>(ap.twiddle) + i);
+    s_g[i] = __ldg(reinterpret_cast<const float *>(ap.gain) + i);
+  }
+  float *s_wt = reinterpret_cast<float *>(smem_raw + fast_wtile_off<N, false>());
+  const long long tile = (long long)blockIdx.y * ap.s_outer + (long long)blockIdx.x * 64;
+  {
+    const float *wt = w + b * ps.w_bs + tile;
+    for (int c = threadIdx.x; c < N * 16; c += NT) {
+      const int row = c >> 4, part = c & 15;
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                       smem_addr(s_wt + row * 64 + part * 4)),
+                   "l"(wt + (long long)row * ap.s_n + part * 4)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  pdl_wait();   // the input is the previous pass's output
+  pdl_release();
+  const long long base = tile + 2 * lane;
+  float2 v[R1];
+  {
+    const float *src = in + b * ps.in_bs[set] + base;
+    reg::static_for<0, R1>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      v[j] = __ldg(reinterpret_cast<const float2 *>(src + (long long)(p + P * j) * ap.s_n));
+    });
+  }
+  __syncthreads();   // the shared tables are complete
+  four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  __syncthreads();   // every thread's tile copies are visible
+  {
+    float *dq = qo + b * ps.qout_bs[set] + base;
+    reg::static_for<0, R1>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      const float2 wv = reinterpret_cast<const float2 *>(s_wt)[(p + P * j) * 32 + lane];
+      float2 r = v[j];
+      r.x *= wv.x;
+      r.y *= wv.y;
+      *reinterpret_cast<float2 *>(dq + (long long)(p + P * j) * ap.s_n) = r;
+      v[j] = make_float2(r.x * wv.x, r.y * wv.y);
+    });
+  }
+  four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
+  float *dst = out + b * ps.out_bs[set] + base;
+  reg::static_for<0, R1>([&](auto j_) {
+    constexpr int j = decltype(j_)::value;
+    *reinterpret_cast<float2 *>(dst + (long long)(p + P * j) * ap.s_n) = v[j];
+  });
+}
+
+// Fused step pair on whole z-planes: x and y filters (finishing step s: the
+// post factor, stored to qout), the factor again, then y and x filters of
+// step s+1 (the filters commute), stored to out.  The plane and the factor's
+// plane (cp.async, issued before the dependency wait) sit in shared memory.
+template <int NX, int NY> constexpr size_t xyxy_wplane_off() {
+  return xy_plane_bytes<NX, NY>();
+}
+template <int NX, int NY, int G> constexpr size_t xyxy_smem() {
+  return xy_plane_bytes<NX, NY>() + (size_t)NX * NY * 4 +
+         (size_t)G * (NX > NY ? NX : NY) * 32 * 8 + (size_t)(NX + NY) * 12;
+}
+
+template <int NX, int NY, int G>
+__global__ void __launch_bounds__(256 * G, 1)
+    k_xyxy(AxisPlan apx, AxisPlan apy, PassSet<float> ps) {
+  constexpr int P = 8, NT = 256 * G, PITCH = NX + 1;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float *plane = reinterpret_cast<float *>(smem_raw);
+  float *wplane = reinterpret_cast<float *>(smem_raw + xyxy_wplane_off<NX, NY>());
+  const int grp = G == 1 ? 0 : (int)(threadIdx.x >> 8);
+  float2 *ex0 = reinterpret_cast<float2 *>(smem_raw + xyxy_wplane_off<NX, NY>() +
+                                           (size_t)NX * NY * 4);
+  float2 *ex = ex0 + grp * (NX > NY ? NX : NY) * 32;
+  float2 *twx = ex0 + G * (NX > NY ? NX : NY) * 32;
+  float2 *twy = twx + NX;
+  float *gx = reinterpret_cast<float *>(twy + NY);
+  float *gy = gx + NX;
+  const int lane = threadIdx.x & 31, p = (threadIdx.x >> 5) & 7;
+  const int bar_id = G == 1 ? 0 : 1 + grp;
+  const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
+  const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
+  const long long base = (long long)blockIdx.x * NX * NY;
+  const float *in = ps.in[set] + b * ps.in_bs[set] + base;
+  float *out = ps.out[set] + b * ps.out_bs[set] + base;
+  float *qo = ps.qout[set] + b * ps.qout_bs[set] + base;
+  const float *w = ps.post[set] + b * ps.w_bs + base;
+  for (int i = threadIdx.x; i < NX; i += NT) {
+    twx[i] = __ldg(reinterpret_cast<const float2 *>(apx.twiddle) + i);
+    gx[i] = __ldg(reinterpret_cast<const float *>(apx.gain) + i);
+  }
+  for (int i = threadIdx.x; i < NY; i += NT) {
+    twy[i] = __ldg(reinterpret_cast<const float2 *>(apy.twiddle) + i);
+    gy[i] = __ldg(reinterpret_cast<const float *>(apy.gain) + i);
+  }
+  for (int c = threadIdx.x; c < NX * NY / 4; c += NT)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(wplane + 4 * c)),
+                 "l"(w + 4 * c)
+                 : "memory");
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  pdl_wait();   // the plane is the previous pass's output
+  pdl_release();
+  constexpr int PER = NX * NY / NT;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int i = threadIdx.x + k * NT;
+    plane[(i / NX) * PITCH + (i % NX)] = __ldg(in + i);
+  }
+  __syncthreads();
+  auto x_pass = [&]() {
+#pragma unroll 1
+    for (int r = grp; r < NY / 64; r += G) {
+      float2 v[NX / P];
+      const int ra = r * 32 + lane, rb = ra + NY / 2;
+      reg::static_for<0, NX / P>([&](auto j_) {
+        constexpr int j = decltype(j_)::value;
+        const int n = p + P * j;
+        v[j] = make_float2(plane[ra * PITCH + n], plane[rb * PITCH + n]);
+      });
+      four_step<NX, P>(v, ex, twx, gx, p, lane, bar_id, []() {});
+      reg::static_for<0, NX / P>([&](auto j_) {
+        constexpr int j = decltype(j_)::value;
+        const int n = p + P * j;
+        plane[ra * PITCH + n] = v[j].x;
+        plane[rb * PITCH + n] = v[j].y;
+      });
+    }
+  };
+  x_pass();
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  __syncthreads();   // rows filtered; the factor's plane is visible
+  // y filter of step s, the factor (qout), the factor again, y filter of s+1
+#pragma unroll 1
+  for (int r = grp; r < NX / 64; r += G) {
+    float2 v[NY / P];
+    const int ca = r * 64 + lane, cb = ca + 32;
+    reg::static_for<0, NY / P>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      const int n = p + P * j;
+      v[j] = make_float2(plane[n * PITCH + ca], plane[n * PITCH + cb]);
+    });
+    four_step<NY, P>(v, ex, twy, gy, p, lane, bar_id, []() {});
+    reg::static_for<0, NY / P>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      const int n = p + P * j;
+      const float wa = wplane[n * NX + ca], wb = wplane[n * NX + cb];
+      const float a = v[j].x * wa, c = v[j].y * wb;
+      qo[n * NX + ca] = a;
+      qo[n * NX + cb] = c;
+      v[j] = make_float2(a * wa, c * wb);
+    });
+    four_step<NY, P>(v, ex, twy, gy, p, lane, bar_id, []() {});
+    reg::static_for<0, NY / P>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      const int n = p + P * j;
+      plane[n * PITCH + ca] = v[j].x;
+      plane[n * PITCH + cb] = v[j].y;
+    });
+  }
+  __syncthreads();
+  x_pass();
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int i = threadIdx.x + k * NT;
+    out[i] = plane[(i / NX) * PITCH + (i % NX)];
+  }
+}
+
 template <int N, int P, bool XP> size_t fast_smem() {
   return XP ? fast_core_smem<N, XP>() + (size_t)N * (sizeof(float2) + sizeof(float))
             : fast_wtile_off<N, XP>() + (size_t)N * 64 * sizeof(float);
@@ -601,7 +792,61 @@ cudaError_t launch_xy_t(const AxisPlan &apx, const AxisPlan &apy, const PassSet<
   return launch_pdl(k_xy_plane<NX, NY, G>, grid, dim3(256 * G), xy_smem<NX, NY, G>(), st, apx,
                     apy, ps);
 }
+template <int NX, int NY> cudaError_t prep_xyxy() {
+  constexpr int G = xy_groups<NX, NY>();
+  return cudaFuncSetAttribute(k_xyxy<NX, NY, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)xyxy_smem<NX, NY, G>());
+}
+template <int NX, int NY>
+cudaError_t launch_xyxy_t(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
+                          cudaStream_t st) {
+  constexpr int G = xy_groups<NX, NY>();
+  dim3 grid(apy.n_outer, 1, ps.nset * ps.batch);   // one CTA per z-plane
+  return launch_pdl(k_xyxy<NX, NY, G>, grid, dim3(256 * G), xyxy_smem<NX, NY, G>(), st, apx,
+                    apy, ps);
+}
+template <int N, int P> cudaError_t prep_zz() {
+  return cudaFuncSetAttribute(k_zz<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)fast_smem<N, P, false>());
+}
+template <int N, int P>
+cudaError_t launch_zz_t(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
+  dim3 grid(ap.n_real / 64, ap.n_outer, ps.nset * ps.batch);
+  return launch_pdl(k_zz<N, P>, grid, dim3(P * 32), fast_smem<N, P, false>(), st, ap, ps);
+}
+// 16-byte cp.async tiles and float2 lines: refuse misaligned buffers
+bool fused_aligned(const PassSet<float> &ps) {
+  for (int k = 0; k < ps.nset; ++k)
+    if ((reinterpret_cast<uintptr_t>(ps.post[k]) | reinterpret_cast<uintptr_t>(ps.in[k]) |
+         reinterpret_cast<uintptr_t>(ps.out[k]) | reinterpret_cast<uintptr_t>(ps.qout[k])) & 15 ||
+        !ps.post[k] || !ps.qout[k])
+      return false;
+  return true;
+}
 }  // namespace
+
+cudaError_t launch_zz(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
+  if (ps.nset < 1 || ps.nset > kMaxSet || ap.n_fast) return cudaErrorInvalidValue;
+  if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
+  switch (ap.n) {
+    case 32: return launch_zz_t<32, 4>(ap, ps, st);
+    case 64: return launch_zz_t<64, 8>(ap, ps, st);
+    case 128: return launch_zz_t<128, 8>(ap, ps, st);
+    case 256: return launch_zz_t<256, 16>(ap, ps, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_xyxy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
+                        cudaStream_t st) {
+  if (ps.nset < 1 || ps.nset > kMaxSet) return cudaErrorInvalidValue;
+  if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
+  if (apx.n == 128 && apy.n == 128) return launch_xyxy_t<128, 128>(apx, apy, ps, st);
+  if (apx.n == 64 && apy.n == 64) return launch_xyxy_t<64, 64>(apx, apy, ps, st);
+  if (apx.n == 128 && apy.n == 64) return launch_xyxy_t<128, 64>(apx, apy, ps, st);
+  if (apx.n == 64 && apy.n == 128) return launch_xyxy_t<64, 128>(apx, apy, ps, st);
+  return cudaErrorInvalidValue;
+}
 
 bool xy_fusable(const AxisPlan &apx, const AxisPlan &apy) {
   return apx.n_fast && !apy.n_fast && (apx.n == 64 || apx.n == 128) &&
@@ -639,6 +884,14 @@ cudaError_t fast_line_prepare() {
   if ((e = prep_xy<64, 64>()) != cudaSuccess) return e;
   if ((e = prep_xy<128, 64>()) != cudaSuccess) return e;
   if ((e = prep_xy<64, 128>()) != cudaSuccess) return e;
+  if ((e = prep_xyxy<128, 128>()) != cudaSuccess) return e;
+  if ((e = prep_xyxy<64, 64>()) != cudaSuccess) return e;
+  if ((e = prep_xyxy<128, 64>()) != cudaSuccess) return e;
+  if ((e = prep_xyxy<64, 128>()) != cudaSuccess) return e;
+  if ((e = prep_zz<32, 4>()) != cudaSuccess) return e;
+  if ((e = prep_zz<64, 8>()) != cudaSuccess) return e;
+  if ((e = prep_zz<128, 8>()) != cudaSuccess) return e;
+  if ((e = prep_zz<256, 16>()) != cudaSuccess) return e;
   return e;
 }
 

@@ -41,6 +41,10 @@ template <typename R> struct PassSet {
   int nset;
   int batch;
   unsigned *err;   // device error word (bounded-wait timeouts), may be null for non-pipelined kernels
+  // fused step pairs only (launch_zz / launch_xyxy): where the finished
+  // propagator slice goes; `out` then receives the next step's intermediate
+  R *qout[kMaxSet];
+  long long qout_bs[kMaxSet];
 };
 
 // Register-resident FP32 pass (k_fast.cu): n in {32, 64, 128, 256} and
@@ -52,6 +56,14 @@ cudaError_t launch_xy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<fl
                       cudaStream_t st);
 cudaError_t fast_line_prepare();
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
+// Fused step pairs.  The axis filters commute, so consecutive contour steps
+// can run their passes in alternating order (x+y then z, z then x+y); the
+// end of one step and the start of the next are then the same pass type and
+// run as one kernel: qout = post * K_a(in), out = K_a(post * qout), with
+// K_a the z filter (launch_zz) or the x+y filters (launch_xyxy).
+cudaError_t launch_zz(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
+cudaError_t launch_xyxy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
+                        cudaStream_t st);
 
 // Generic mixed-radix Stockham line filter (any n whose prime factors are
 // <= 61).  in/out may not alias.  pre multiplies the input, post the output
