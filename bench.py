@@ -37,6 +37,14 @@ WORKLOAD = ("128^3 periodic grid, double-gyroid init chiN*0.2*g(r)+N(0,0.02) see
             "f=0.36, chiN=18, box 3.8 Rg, Ns=200 (ds=0.005, NsA=72, dNsB=128), "
             "1 SCF iteration (4 propagator marches + Q + phi + simple mixing) per step")
 BYTES_PER_PT_STEP = {"fp32": 12.0, "fp64": 24.0}
+# DRAM bytes (read + write) of one march launch = one contour step of one
+# propagator at 128^3 FP32, from an ncu capture with warm L2 (--cache-control
+# none): the slice's write-back only, against 25.2 MB of algorithmic bytes --
+# the other operands stay in L2.
+TRAFFIC_PER_STEP = 8.48e6
+TRAFFIC_NOTE = ("dram bytes per launch (one contour step) with warm L2, mean of 4 launches of "
+                "k_xyxy/k_zz from one ncu capture of the Ns=20 case; algorithmic bytes per "
+                "launch: 12 B x 128^3 = 25.2 MB")
 
 
 def dist_env():
@@ -515,9 +523,13 @@ def run_ours(args):
                                                      (4 if args.precision == "fp32" else 8) / 1e9),
                        "parallelism": f"replicas x{ws} (no exchange step)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": TRAFFIC_PER_STEP if (headline and args.precision == "fp32")
+                         else None,
+                         "traffic_note": TRAFFIC_NOTE,
                          "peak_kind": peak_kind,
-                         "kernel": "propagator march (sovDifFft): per-axis line-filter passes",
+                         "kernel": "propagator march (sovDifFft): one fused launch per contour "
+                                   "step at 128^3 (k_xyxy / k_zz alternating)",
                          "bytes_per_point_step": bpp,
                          "march_ms_avg": march_ms / max(n_marches, 1),
                          "marches_timed": n_marches},
