@@ -240,7 +240,67 @@ int run_chains(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nch
 // odd and (z, x+y) when k is even, which the commuting axis filters allow.
 // The end of step k and the start of step k+1 are then one kernel
 // (k_zz / k_xyxy): one launch per contour step instead of two.
+// Without the x+y plane (three passes, all register-resident) the same idea
+// gives (x, y, z) for odd and (z, y, x) for even steps: k_zz / k_xx fuse the
+// end of one step with the start of the next, two launches per step instead
+// of three.
+bool fused_possible(const scft_ctx *ctx) {
+  if (!ctx->fuse_steps || ctx->rbytes != 4 || ctx->passes.size() != 3) return false;
+  if (ctx->fuse_xy) return ctx->passes[2].use_fast != 0;
+  return ctx->passes[0].use_fast && ctx->passes[1].use_fast && ctx->passes[2].use_fast;
+}
+
+int run_chain_fused_axes(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t st, int cidx) {
+  const long long M = ctx->M;
+  float *tmp[2] = {static_cast<float *>(ctx->tmp[2 * cidx]),
+                   static_cast<float *>(ctx->tmp[2 * cidx + 1])};
+  const AxisPlan &apx = ctx->passes[0], &apy = ctx->passes[1], &apz = ctx->passes[2];
+  for (int k = 0; k < nseg; ++k) {
+    const Seg &sg = segs[k];
+    int rc = seg_boundary<float>(ctx, sg, st);
+    if (rc) return rc;
+    if (sg.ns == 0) continue;
+    float *q = static_cast<float *>(ctx->q[sg.qi]);
+    const long long qbs = (long long)(ctx->q_ns[sg.qi] + 1) * M;
+    const float *W = static_cast<const float *>(ctx->W[sg.wf]);
+    auto slice = [&](int it) { return q + (long long)(sg.sign > 0 ? it : sg.ns - it) * M; };
+    scft::PassSet<float> ps;
+    auto reset = [&](const float *in, long long in_bs, float *out, long long out_bs) {
+      memset(&ps, 0, sizeof(ps));
+      ps.nset = 1;
+      ps.batch = ctx->batch;
+      ps.w_bs = M;
+      ps.in[0] = in;
+      ps.in_bs[0] = in_bs;
+      ps.out[0] = out;
+      ps.out_bs[0] = out_bs;
+    };
+    // step 1: x with the pre factor, then y; tmp[0] holds the state between steps
+    reset(slice(0), qbs, tmp[1], M);
+    ps.pre[0] = W;
+    if ((rc = launch_set<float>(ctx, apx, ps, st))) return rc;
+    reset(tmp[1], M, tmp[0], M);
+    if ((rc = launch_set<float>(ctx, apy, ps, st))) return rc;
+    for (int it = 2; it <= sg.ns; ++it) {
+      // finish step it-1 (z when it was odd, x when even) and start step it
+      reset(tmp[0], M, tmp[1], M);
+      ps.qout[0] = slice(it - 1);
+      ps.qout_bs[0] = qbs;
+      ps.post[0] = W;
+      if ((it - 1) & 1) CKL(scft::launch_zz(apz, ps, st));
+      else CKL(scft::launch_xx(apx, ps, st));
+      reset(tmp[1], M, tmp[0], M);
+      if ((rc = launch_set<float>(ctx, apy, ps, st))) return rc;
+    }
+    reset(tmp[0], M, slice(sg.ns), qbs);
+    ps.post[0] = W;
+    if ((rc = launch_set<float>(ctx, (sg.ns & 1) ? apz : apx, ps, st))) return rc;
+  }
+  return SCFT_OK;
+}
+
 int run_chain_fused(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t st, int cidx) {
+  if (!ctx->fuse_xy) return run_chain_fused_axes(ctx, segs, nseg, st, cidx);
   const long long M = ctx->M;
   float *tmp[2] = {static_cast<float *>(ctx->tmp[2 * cidx]),
                    static_cast<float *>(ctx->tmp[2 * cidx + 1])};
@@ -303,7 +363,7 @@ int run_chain_fused(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t st, i
 
 int run_chains_any(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nchain,
                    cudaStream_t st, int chain_base = 0) {
-  if (nchain == 1 && ctx->fuse_steps && ctx->rbytes == 4)
+  if (nchain == 1 && fused_possible(ctx))
     return run_chain_fused(ctx, chains[0], nseg[0], st, chain_base);
   return ctx->rbytes == 4 ? run_chains<float>(ctx, chains, nseg, nchain, st, chain_base)
                           : run_chains<double>(ctx, chains, nseg, nchain, st, chain_base);
@@ -611,7 +671,8 @@ int autotune(scft_ctx *ctx) {
   bool has_fast_col = false;
   for (size_t i = 1; i < ctx->passes.size(); ++i) has_fast_col |= ctx->passes[i].use_fast != 0;
   const bool can_xy = ctx->fuse_xy;
-  const bool can_fs = ctx->fuse_steps;
+  const bool can_fs = (ctx->p.flags & SCFT_FLAG_NO_FUSED_STEPS) == 0 && ctx->rbytes == 4 &&
+                      ctx->passes.size() == 3;
   int rc;
   if ((rc = boltzmann(ctx, SCFT_FIELD_WA, ctx->st))) return rc;
   if ((rc = boltzmann(ctx, SCFT_FIELD_WB, ctx->st))) return rc;
@@ -625,13 +686,14 @@ int autotune(scft_ctx *ctx) {
     for (int xy = 0; xy < (can_xy ? 2 : 1); ++xy)
       for (int pipe = 0; pipe < (has_fast_col ? 2 : 1); ++pipe)
       for (int fs = 0; fs < (can_fs ? 2 : 1); ++fs) {
-        // fused step pairs run only on two-stream chains with the x+y plane
-        // and the plain column kernels
-        if (fs && (!two || !xy || pipe)) continue;
+        // fused step pairs run only on two-stream chains and the plain column
+        // kernels (with the x+y plane, or with three register-resident passes)
+        if (fs && (!two || pipe)) continue;
         ctx->two_streams = two;
         ctx->fuse_xy = can_xy && xy;
         ctx->use_pipe = pipe;
         ctx->fuse_steps = fs;
+        if (fs && !fused_possible(ctx)) continue;
         if (ctx->march_exec) cudaGraphExecDestroy(ctx->march_exec);
         ctx->march_exec = nullptr;
         if ((rc = march_phase_graph(ctx))) break;   // capture + warm-up
@@ -923,9 +985,10 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   ctx->fuse_xy = rb == 4 && (p.flags & SCFT_FLAG_NO_XY) == 0 && ctx->passes.size() >= 2 &&
                  axes[0] == 0 && axes[1] == 1 &&
                  scft::xy_fusable(ctx->passes[0], ctx->passes[1]);
-  // fused step pairs need the x+y plane kernel and a register-resident z pass
-  ctx->fuse_steps = ctx->fuse_xy && ctx->passes.size() == 3 && ctx->passes[2].use_fast &&
-                    (p.flags & SCFT_FLAG_NO_FUSED_STEPS) == 0;
+  // fused step pairs need three passes: the x+y plane kernel and a
+  // register-resident z pass, or three register-resident axis passes
+  ctx->fuse_steps = (p.flags & SCFT_FLAG_NO_FUSED_STEPS) == 0;
+  ctx->fuse_steps = fused_possible(ctx);
   // With fused step pairs the two-stream chains win at every size the plane
   // kernel takes (measured per SCF iteration: 64^3 1.12 ms against 1.27 ms
   // lockstep, 128^3 4.46 ms against 5.79 ms).

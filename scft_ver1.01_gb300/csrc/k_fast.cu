@@ -604,6 +604,89 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<float> ps) {
   });
 }
 
+// Fused step pair on x lines (rows contiguous, as the x branch of
+// k_fast_line: 64 rows per CTA staged through shared memory, pitch N+1).
+// The factor's tile (64 rows x N, contiguous in memory) is copied with
+// cp.async before the dependency wait.
+template <int N> constexpr size_t xx_wtile_off() { return fast_wtile_off<N, true>(); }
+template <int N> constexpr size_t xx_smem() { return xx_wtile_off<N>() + (size_t)64 * N * 4; }
+
+template <int N, int P>
+__global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<float> ps) {
+  constexpr int R1 = N / P;
+  constexpr int NT = P * 32;
+  constexpr int PITCH = N + 1;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float2 *ex = reinterpret_cast<float2 *>(smem_raw);   // aliases the staging tile
+  float *stg = reinterpret_cast<float *>(smem_raw);
+  const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
+  const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
+  const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
+  float2 *s_tw = reinterpret_cast<float2 *>(smem_raw + fast_core_smem<N, true>());
+  float *s_g = reinterpret_cast<float *>(s_tw + N);
+  for (int i = threadIdx.x; i < N; i += NT) {
+    s_tw[i] = __ldg(reinterpret_cast<const float2 *>(ap.twiddle) + i);
+    s_g[i] = __ldg(reinterpret_cast<const float *>(ap.gain) + i);
+  }
+  const long long base = (long long)blockIdx.x * 64 * N;   // 64 consecutive rows
+  float *s_wt = reinterpret_cast<float *>(smem_raw + xx_wtile_off<N>());
+  {
+    const float *wt = ps.post[set] + b * ps.w_bs + base;
+    for (int c = threadIdx.x; c < 16 * N; c += NT)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(s_wt + 4 * c)),
+                   "l"(wt + 4 * c)
+                   : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  pdl_wait();   // the rows are the previous pass's output
+  pdl_release();
+  const float *src = ps.in[set] + b * ps.in_bs[set] + base;
+#pragma unroll
+  for (int i = threadIdx.x; i < 64 * N; i += NT) stg[(i / N) * PITCH + (i % N)] = __ldg(src + i);
+  __syncthreads();
+  float2 v[R1];
+  auto rows_to_regs = [&]() {
+    reg::static_for<0, R1>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      const int n = p + P * j;
+      v[j] = make_float2(stg[lane * PITCH + n], stg[(lane + 32) * PITCH + n]);
+    });
+    __syncthreads();   // the staging tile is free for the exchange
+  };
+  auto regs_to_rows = [&]() {
+    reg::static_for<0, R1>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      const int n = p + P * j;
+      stg[lane * PITCH + n] = v[j].x;
+      stg[(lane + 32) * PITCH + n] = v[j].y;
+    });
+    __syncthreads();
+  };
+  rows_to_regs();
+  four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
+  regs_to_rows();
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  __syncthreads();   // every thread's tile copies are visible
+  {
+    float *dq = ps.qout[set] + b * ps.qout_bs[set] + base;
+#pragma unroll 4
+    for (int i = threadIdx.x; i < 64 * N; i += NT) {
+      const int o = (i / N) * PITCH + (i % N);
+      const float w = s_wt[i];
+      const float x = stg[o] * w;
+      dq[i] = x;
+      stg[o] = x * w;
+    }
+  }
+  __syncthreads();
+  rows_to_regs();
+  four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
+  regs_to_rows();
+  float *dst = ps.out[set] + b * ps.out_bs[set] + base;
+#pragma unroll 4
+  for (int i = threadIdx.x; i < 64 * N; i += NT) dst[i] = stg[(i / N) * PITCH + (i % N)];
+}
+
 // Fused step pair on whole z-planes: x and y filters (finishing step s: the
 // post factor, stored to qout), the factor again, then y and x filters of
 // step s+1 (the filters commute), stored to out.  The plane and the factor's
@@ -805,6 +888,15 @@ cudaError_t launch_xyxy_t(const AxisPlan &apx, const AxisPlan &apy, const PassSe
   return launch_pdl(k_xyxy<NX, NY, G>, grid, dim3(256 * G), xyxy_smem<NX, NY, G>(), st, apx,
                     apy, ps);
 }
+template <int N, int P> cudaError_t prep_xx() {
+  return cudaFuncSetAttribute(k_xx<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)xx_smem<N>());
+}
+template <int N, int P>
+cudaError_t launch_xx_t(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
+  dim3 grid(ap.n_real / 64, 1, ps.nset * ps.batch);
+  return launch_pdl(k_xx<N, P>, grid, dim3(P * 32), xx_smem<N>(), st, ap, ps);
+}
 template <int N, int P> cudaError_t prep_zz() {
   return cudaFuncSetAttribute(k_zz<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)fast_smem<N, P, false>());
@@ -824,6 +916,18 @@ bool fused_aligned(const PassSet<float> &ps) {
   return true;
 }
 }  // namespace
+
+cudaError_t launch_xx(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
+  if (ps.nset < 1 || ps.nset > kMaxSet || !ap.n_fast) return cudaErrorInvalidValue;
+  if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
+  switch (ap.n) {
+    case 32: return launch_xx_t<32, 4>(ap, ps, st);
+    case 64: return launch_xx_t<64, 8>(ap, ps, st);
+    case 128: return launch_xx_t<128, 8>(ap, ps, st);
+    case 256: return launch_xx_t<256, 16>(ap, ps, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 cudaError_t launch_zz(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
   if (ps.nset < 1 || ps.nset > kMaxSet || ap.n_fast) return cudaErrorInvalidValue;
@@ -888,6 +992,10 @@ cudaError_t fast_line_prepare() {
   if ((e = prep_xyxy<64, 64>()) != cudaSuccess) return e;
   if ((e = prep_xyxy<128, 64>()) != cudaSuccess) return e;
   if ((e = prep_xyxy<64, 128>()) != cudaSuccess) return e;
+  if ((e = prep_xx<32, 4>()) != cudaSuccess) return e;
+  if ((e = prep_xx<64, 8>()) != cudaSuccess) return e;
+  if ((e = prep_xx<128, 8>()) != cudaSuccess) return e;
+  if ((e = prep_xx<256, 16>()) != cudaSuccess) return e;
   if ((e = prep_zz<32, 4>()) != cudaSuccess) return e;
   if ((e = prep_zz<64, 8>()) != cudaSuccess) return e;
   if ((e = prep_zz<128, 8>()) != cudaSuccess) return e;

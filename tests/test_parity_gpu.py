@@ -240,3 +240,27 @@ def test_field_view_is_zero_copy(pkg):
         v.mul_(2.0)
         torch.cuda.synchronize()
         assert np.array_equal(ctx.wa, 2.0 * wa)
+
+
+@pytest.mark.parametrize("flags", ["default", "NO_XY", "NO_FUSED_STEPS", "LOCKSTEP"])
+@pytest.mark.parametrize("g", [(64, 64, 64, 3.8, 3.8, 3.8), (128, 64, 32, 4.2, 3.0, 2.0),
+                               (256, 64, 32, 8.0, 3.0, 2.0)])
+def test_march_schedules_match_oracle(pkg, orc, g, flags):
+    """Every FP32 march schedule (fused step pairs with the x+y plane or with
+    three axis passes, unfused, lockstep) against the oracle, over several
+    SCF iterations (the fused order changes only FP32 rounding)."""
+    from scft_gb300 import fields
+    kw = dict(hAB=18.0, fA=0.36, ds0=0.02)
+    p = oparams(orc, g, batch=1, **kw)
+    wa, wb = fields.gyroid(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 18.0, seed=4)
+    f = 0 if flags == "default" else getattr(pkg, "FLAG_" + flags)
+    with make_ctx(pkg, g, 1, batch=1, flags=f, **kw) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.get_conc()
+        pha, Q = ctx.pha, ctx.Q()
+        sched, _ = ctx.schedule()
+    ref = orc.get_conc(wa, wb, p)
+    assert rel(pha, ref.pha) < TOL[1]
+    assert rel(Q, ref.Q) < TOL[1]
+    if flags == "default":
+        assert not sched & pkg.FLAG_NO_FUSED_STEPS
