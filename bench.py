@@ -219,6 +219,7 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
         it64, fe64, ok64 = converge_timed(c64, tol, max_it, budget_s)
         t64 = time.perf_counter() - t0
         r64 = float(c64.residual()[0][0])
+        pha64, Q64 = c64.pha, c64.Q()
     with pkg.Context(precision=pkg.PREC_FP32, **kw) as c32, \
             pkg.Context(precision=pkg.PREC_FP64, **kw) as pol:
         c32.set_w(wa, wb)
@@ -234,13 +235,17 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
         itp, fep, okp = converge_timed(pol, tol, max_it, budget_s)
         tmx = time.perf_counter() - t0
         rmx = float(pol.residual()[0][0])
+        phamx, Qmx = pol.pha, pol.Q()
     out.update(fp64={"seconds": t64, "iterations": it64, "F": fe64[0, 0], "residual": r64,
                      "converged": ok64},
                fp32_fp64_polish={"seconds": tmx, "iterations_fp32": it32,
                                  "iterations_fp64_polish": itp, "F": fep[0, 0],
                                  "residual": rmx, "converged": okp},
                speedup=t64 / tmx if tmx > 0 else None,
-               F_abs_diff=abs(fep[0, 0] - fe64[0, 0]))
+               F_abs_diff=abs(fep[0, 0] - fe64[0, 0]),
+               # phi and Q of the last getConc of each run (both converged)
+               phiA_rel_diff=float(np.abs(phamx - pha64).max() / np.abs(pha64).max()),
+               Q_rel_diff=float(abs(Qmx[0] - Q64[0]) / abs(Q64[0])))
     return out
 
 
