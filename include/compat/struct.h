@@ -9,7 +9,9 @@
  *   - wa_cu/wb_cu/pha_cu/phb_cu are FP64 [batch][Nz][Ny][Nx] device arrays;
  *   - qa_cu/qb_cu/qca_cu/qcb_cu point at contour-outer propagator storage
  *     ([batch][s][Nz][Ny][Nx], FP64 or FP32), not the reference's s-fastest
- *     g[b][r][s];
+ *     g[b][r][s] -- unless the driver is compiled with
+ *     -DSCFT_COMPAT_FP64_LAYOUT: then they point at FP64 mirrors in the
+ *     reference's layout, refreshed by getConc and sovDifFft;
  *   - ql/ffl hold host arrays (batch doubles), refreshed by getConc;
  *   - plan_forward/plan_backward/device_in/device_out/kxyzdz_cu are unused
  *     (the FFTs are the library's own kernels).
@@ -25,6 +27,12 @@
 #include "../scft_capi.h"
 
 #define Pi 3.1415926535
+
+#ifdef SCFT_COMPAT_FP64_LAYOUT
+#define SCFT_COMPAT_REFERENCE_LAYOUT 1
+#else
+#define SCFT_COMPAT_REFERENCE_LAYOUT 0
+#endif
 
 typedef struct {
   int kernal_type;   /* 1 GPU, 2 CPU (not available), -1 unset */
@@ -78,6 +86,9 @@ typedef struct {
   /* GB300 build: the context behind the fields above */
   scft_ctx *gb300;
   int precision;     /* SCFT_PREC_FP64 (default) or SCFT_PREC_FP32 */
+  /* 1: qa_cu/qb_cu/qca_cu/qcb_cu are FP64 mirrors in the reference's
+   * g[b][r][s] layout (set by -DSCFT_COMPAT_FP64_LAYOUT in the driver) */
+  int reference_layout = SCFT_COMPAT_REFERENCE_LAYOUT;
 } CUFFT_INFO;
 
 #endif

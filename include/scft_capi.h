@@ -148,6 +148,13 @@ int scft_set_qint(scft_ctx *ctx, int q, int s);
  * dst holds batch*M doubles. */
 int scft_get_q(scft_ctx *ctx, int q, int s, double *dst);
 
+/* The whole propagator q in the reference's own layout g[b][r][s] (s
+ * fastest, FP64; cuda_aid.cu:237), written to caller-owned device memory of
+ * batch*M*(ns_q+1) doubles by a tiled transpose.  The struct API keeps its
+ * qa_cu/qb_cu/qca_cu/qcb_cu in this layout when built with
+ * -DSCFT_COMPAT_FP64_LAYOUT. */
+int scft_copy_q_reference_layout(scft_ctx *ctx, int q, double *dst_device);
+
 /* getConc (cuda_scft.cu:61-138): average_value(wa), the four marches, Q and
  * the trapezoid contour sums giving pha/phb.  Stays on the device. */
 int scft_get_conc(scft_ctx *ctx);

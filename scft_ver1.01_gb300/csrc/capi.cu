@@ -1194,6 +1194,22 @@ int scft_set_box(scft_ctx *ctx, double lx, double ly, double lz) {
   return upload_gains(ctx);
 }
 
+int scft_copy_q_reference_layout(scft_ctx *ctx, int q, double *dst_device) {
+  if (!ctx || !dst_device || q < 0 || q > 3)
+    return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad propagator or null pointer");
+  CK(cudaSetDevice(ctx->p.device));
+  if (ctx->rbytes == 4)
+    CKL(scft::launch_q_to_reference_layout<float>(static_cast<const float *>(ctx->q[q]),
+                                                  ctx->q_ns[q], ctx->M, ctx->batch, dst_device,
+                                                  ctx->st));
+  else
+    CKL(scft::launch_q_to_reference_layout<double>(static_cast<const double *>(ctx->q[q]),
+                                                   ctx->q_ns[q], ctx->M, ctx->batch, dst_device,
+                                                   ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return SCFT_OK;
+}
+
 int scft_field_device_ptr(scft_ctx *ctx, int field, double **dptr) {
   if (!ctx || !dptr) return SCFT_ERR_INVALID_ARG;
   double *p = field_ptr(ctx, field);

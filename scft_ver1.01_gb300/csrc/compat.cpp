@@ -46,6 +46,13 @@ int field_of(CUFFT_INFO *c, double *p) {
   if (!c->wb_cu.empty() && p == c->wb_cu[0]) return SCFT_FIELD_WB;
   return -1;
 }
+// Refresh the reference-layout mirror of propagator q (no-op without them).
+void refresh_mirror(CUFFT_INFO *c, int q) {
+  if (!c->reference_layout) return;
+  std::vector<double *> *mir[4] = {&c->qa_cu, &c->qcb_cu, &c->qb_cu, &c->qca_cu};
+  report(c->gb300, scft_copy_q_reference_layout(c->gb300, q, (*mir[q])[0]), "reference layout");
+}
+
 int prop_of(CUFFT_INFO *c, double *p) {
   if (!c->qa_cu.empty() && p == c->qa_cu[0]) return SCFT_Q_A;
   if (!c->qcb_cu.empty() && p == c->qcb_cu[0]) return SCFT_Q_CB;
@@ -66,7 +73,11 @@ int largest_divisor_1024(long n) {
 // init.cpp:8-132
 int init_scft(CUFFT_INFO *cufft_info, GPU_INFO *gpu_info, int argc, char **argv) {
   memset(gpu_info, 0, sizeof(*gpu_info));
+  // the layout choice comes from the driver's own compilation of struct.h
+  // (its default member initializer), so it survives the reset
+  const int layout = cufft_info->reference_layout == 1 ? 1 : 0;
   new (cufft_info) CUFFT_INFO();
+  cufft_info->reference_layout = layout;
   gpu_info->kernal_type = -1;
   const char *type = flag_value(argc, argv, "kernal");
   cufft_info->MaxIT = flag_int(argc, argv, "step");
@@ -218,6 +229,24 @@ void initialize_cufft(GPU_INFO *gpu_info, CUFFT_INFO *c) {
   c->qcb_cu.assign(1, static_cast<double *>(ctx->q[SCFT_Q_CB]));
   c->qb_cu.assign(1, static_cast<double *>(ctx->q[SCFT_Q_B]));
   c->qca_cu.assign(1, static_cast<double *>(ctx->q[SCFT_Q_CA]));
+  if (c->reference_layout) {
+    // FP64 mirrors in the reference's g[b][r][s] layout (init_cuda.cu:522-526)
+    std::vector<double *> *mir[4] = {&c->qa_cu, &c->qcb_cu, &c->qb_cu, &c->qca_cu};
+    double *m[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool ok = true;
+    for (int q = 0; q < 4 && ok; ++q)
+      ok = cudaMalloc(&m[q], sizeof(double) * ctx->M * ctx->batch * (ctx->q_ns[q] + 1)) ==
+           cudaSuccess;
+    if (ok) {
+      for (int q = 0; q < 4; ++q) mir[q]->assign(1, m[q]);
+    } else {
+      cudaGetLastError();
+      for (double *p : m) cudaFree(p);
+      fprintf(stderr, "initialize_cufft: cannot allocate the reference-layout propagators; "
+                      "keeping the contour-outer ones\n");
+      c->reference_layout = 0;
+    }
+  }
   c->qInt_cu.assign(1, static_cast<double *>(ctx->qint));
   c->wdz_cu.assign(1, static_cast<double *>(ctx->W[0]));
   c->ql.assign(1, (double *)calloc(c->batch, sizeof(double)));
@@ -250,6 +279,7 @@ void sovDifFft(GPU_INFO *gpu_info, CUFFT_INFO *c, std::vector<double *> g,
   }
   report(c->gb300, scft_sov_dif_fft(c->gb300, q, f, ns, sign), "sovDifFft");
   scft_synchronize(c->gb300);
+  refresh_mirror(c, q);
 }
 
 // cuda_scft.cu:61-138
@@ -257,6 +287,7 @@ void getConc(GPU_INFO *gpu_info, CUFFT_INFO *c) {
   (void)gpu_info;
   if (!c->gb300) return;
   report(c->gb300, scft_get_conc(c->gb300), "getConc");
+  for (int q = 0; q < 4; ++q) refresh_mirror(c, q);
   if (scft_get_Q(c->gb300, c->ql[0]) == SCFT_OK)
     for (int i = 0; i < c->batch; ++i) c->ffl[0][i] = c->ds0 / c->ql[0][i];
 }
@@ -294,6 +325,11 @@ void fft_test(GPU_INFO *gpu_info, CUFFT_INFO *c) {
 
 // init_cuda.cu:551-628
 void finalize_cufft(GPU_INFO *gpu_info, CUFFT_INFO *c) {
+  if (c->reference_layout && c->gb300) {
+    std::vector<double *> *mir[4] = {&c->qa_cu, &c->qcb_cu, &c->qb_cu, &c->qca_cu};
+    for (auto *m : mir)
+      if (!m->empty()) cudaFree((*m)[0]);
+  }
   if (c->gb300) scft_destroy(c->gb300);
   c->gb300 = nullptr;
   free(c->wa); free(c->wb); free(c->pha); free(c->phb);

@@ -225,6 +225,31 @@ __global__ void k_phi_w_constrained_ex(double *__restrict__ wa, double *__restri
   }
 }
 
+// Contour-outer propagator [b][s][M] (working precision) -> the reference's
+// layout g[b][r][s] in FP64, s fastest (cuda_aid.cu:237), by 32x32 tiles
+// through shared memory so both sides stay coalesced.
+template <typename R>
+__global__ void k_q_to_reference_layout(const R *__restrict__ q, int ns1, long long M,
+                                        double *__restrict__ g) {
+  __shared__ double tile[32][33];
+  const long long b = blockIdx.z;
+  const long long r0 = (long long)blockIdx.x * 32;
+  const int s0 = blockIdx.y * 32;
+  const R *qb = q + b * ns1 * M;
+  double *gb = g + b * ns1 * M;
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int s = s0 + k;
+    const long long r = r0 + threadIdx.x;
+    if (s < ns1 && r < M) tile[k][threadIdx.x] = (double)qb[(long long)s * M + r];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const long long r = r0 + k;
+    const int s = s0 + threadIdx.x;
+    if (s < ns1 && r < M) gb[r * ns1 + s] = tile[threadIdx.x][k];
+  }
+}
+
 // partial layout: [b][3][nblk]
 __global__ void k_fe_partials(const double *__restrict__ wa, const double *__restrict__ wb,
                               const double *__restrict__ pha, const double *__restrict__ phb,
@@ -345,6 +370,20 @@ cudaError_t launch_phi_w(double *wa, double *wb, const double *pha, const double
   k_phi_w<<<grid_for(n), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, wopt, wcmp, n);
   return cudaGetLastError();
 }
+template <typename R>
+cudaError_t launch_q_to_reference_layout(const R *q, int ns, long long M, int batch, double *g,
+                                         cudaStream_t st) {
+  const long long gx = (M + 31) / 32;
+  if (gx > 0x7fffffffLL || batch > 65535) return cudaErrorInvalidValue;
+  dim3 grid((unsigned)gx, (unsigned)((ns + 1 + 31) / 32), batch);
+  k_q_to_reference_layout<R><<<grid, dim3(32, 8), 0, st>>>(q, ns + 1, M, g);
+  return cudaGetLastError();
+}
+template cudaError_t launch_q_to_reference_layout<float>(const float *, int, long long, int,
+                                                         double *, cudaStream_t);
+template cudaError_t launch_q_to_reference_layout<double>(const double *, int, long long, int,
+                                                          double *, cudaStream_t);
+
 cudaError_t launch_phi_w_constrained(double *wa, double *wb, const double *pha, const double *phb,
                                      const double *target, double hAB, double lambda, int ex,
                                      long long M, int batch, cudaStream_t st) {

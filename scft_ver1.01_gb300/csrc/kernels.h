@@ -134,6 +134,10 @@ cudaError_t launch_contour_phi(const R *q, const R *qc, int ns, long long M, int
 cudaError_t launch_phi_w(double *wa, double *wb, const double *pha, const double *phb,
                          double hAB, double wopt, double wcmp, long long M, int batch,
                          cudaStream_t st);
+// propagator [b][s][M] -> g[b][r][s] FP64 (the reference's layout)
+template <typename R>
+cudaError_t launch_q_to_reference_layout(const R *q, int ns, long long M, int batch, double *g,
+                                         cudaStream_t st);
 // phi_w_constrained (ex == 0) / phi_w_constrainedEx (ex != 0)
 cudaError_t launch_phi_w_constrained(double *wa, double *wb, const double *pha, const double *phb,
                                      const double *target, double hAB, double lambda, int ex,

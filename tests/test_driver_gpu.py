@@ -66,3 +66,29 @@ def test_driver_missing_config(pkg, tmp_path):
                        timeout=120)
     assert r.returncode != 0
     assert "ab.txt did not exist" in r.stdout
+
+
+def test_struct_api_reference_layout(pkg, orc, tmp_path):
+    """A driver built with -DSCFT_COMPAT_FP64_LAYOUT sees qa_cu/qcb_cu in the
+    reference's g[b][r][s] FP64 layout after getConc (cuda_aid.cu:237)."""
+    import shutil
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    pkgdir = os.path.join(ROOT, "scft_ver1.01_gb300")
+    exe = str(tmp_path / "layout_check")
+    r = subprocess.run([nvcc, "-std=c++17", "-DSCFT_COMPAT_FP64_LAYOUT",
+                        "-I" + os.path.join(ROOT, "include", "compat"),
+                        "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "native", "compat_layout_check.cpp"),
+                        "-L" + pkgdir, "-lscft_gb300", "-Xlinker", "-rpath=" + pkgdir, "-o", exe],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    from scft_gb300 import fields
+    p = orc.Params(nx=16, ny=12, nz=8, lx=4.0, ly=3.0, lz=2.0, hAB=20.0, fA=0.4, ds0=0.02,
+                   batch=2)
+    wa, wb = fields.lamellar(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 20.0, seed=3, batch=2)
+    d = str(tmp_path)
+    write_case(orc, d, p, wa, wb)
+    r = subprocess.run([exe], cwd=d, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    line = [l for l in r.stdout.splitlines() if l.startswith("layout_maxdiff=")][0]
+    assert line == "layout_maxdiff=0 reference_layout=1", line
