@@ -344,6 +344,34 @@ int scft_relax_cell(scft_ctx *ctx, int axes_mask, double tol_w, double tol_stres
                     int max_outer, int max_inner, double step0, int *outer_iters,
                     double *dF_dL, double *out5);
 
+/* ---- cubic interpolating spline (spline.h / spline.c) -------------------
+ * The Forsythe-Malcolm-Moler spline of the reference with its optional
+ * known end slopes; same arguments and meaning, bit-identical results.  The
+ * reference's own names are available from include/compat/spline.h. */
+
+/* spline (spline.c:24-210): coefficients b, c, d (each n long) of the spline
+ * through (x[i], y[i]); end1/end2 = 1 imposes slope1/slope2 at the ends,
+ * 0 the default end conditions.  *iflag = 0 ok, 1 fewer than two knots,
+ * 2 x not strictly increasing.  Returns SCFT_OK (or SCFT_ERR_INVALID_ARG for
+ * null pointers). */
+int scft_spline(int n, int end1, int end2, double slope1, double slope2, const double *x,
+                const double *y, double *b, double *c, double *d, int *iflag);
+/* seval (spline.c:213-278): S(u); *last is the segment hint, updated. */
+double scft_spline_eval(int n, double u, const double *x, const double *y, const double *b,
+                        const double *c, const double *d, int *last);
+/* deriv (spline.c:281-347): S'(u). */
+double scft_spline_deriv(int n, double u, const double *x, const double *b, const double *c,
+                         const double *d, int *last);
+/* sinteg (spline.c:351-433): the integral of S from x[0] to u. */
+double scft_spline_integral(int n, double u, const double *x, const double *y, const double *b,
+                            const double *c, const double *d, int *last);
+/* Batched evaluation on the device (no reference counterpart): out[k] =
+ * S(u[k]) (mode 0), S'(u[k]) (mode 1) or the integral to u[k] (mode 2); all
+ * pointers are device memory; enqueued on `stream` (a cudaStream_t). */
+int scft_spline_eval_device(int n, const double *x, const double *y, const double *b,
+                            const double *c, const double *d, const double *u, double *out,
+                            long long count, int mode, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

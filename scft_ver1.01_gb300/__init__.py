@@ -42,7 +42,8 @@ EXPORTS = [
     "scft_get_schedule", "scft_write_vtk", "scft_convert_pha_to_vtk", "scft_set_target",
     "scft_phi_w_constrained", "scft_set_box", "scft_stress", "scft_adjoint",
     "scft_adjoint_checkpoints", "scft_relax_cell", "scft_get_box", "scft_field_device_ptr",
-    "scft_get_stream", "scft_copy_q_reference_layout",
+    "scft_get_stream", "scft_copy_q_reference_layout", "scft_spline", "scft_spline_eval",
+    "scft_spline_deriv", "scft_spline_integral", "scft_spline_eval_device",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
 FLAG_AUTOTUNE, FLAG_NO_FUSED_STEPS = 32, 64
@@ -132,6 +133,16 @@ def load_library(path: str | None = None):
         "scft_field_device_ptr": (C.c_int, [vp, C.c_int, C.POINTER(dp)]),
         "scft_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
         "scft_copy_q_reference_layout": (C.c_int, [vp, C.c_int, vp]),
+        "scft_spline": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp,
+                                  dp, dp, C.POINTER(C.c_int)]),
+        "scft_spline_eval": (C.c_double, [C.c_int, C.c_double, dp, dp, dp, dp, dp,
+                                          C.POINTER(C.c_int)]),
+        "scft_spline_deriv": (C.c_double, [C.c_int, C.c_double, dp, dp, dp, dp,
+                                           C.POINTER(C.c_int)]),
+        "scft_spline_integral": (C.c_double, [C.c_int, C.c_double, dp, dp, dp, dp, dp,
+                                              C.POINTER(C.c_int)]),
+        "scft_spline_eval_device": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_longlong,
+                                              C.c_int, vp]),
         "scft_stress": (C.c_int, [vp, dp]),
         "scft_adjoint": (C.c_int, [vp, dp, dp, dp, dp, dp, dp, C.c_int]),
         "scft_adjoint_checkpoints": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int),
@@ -176,6 +187,56 @@ def convert_pha_to_vtk(pha_path: str, vtk_path: str):
     st = lib.scft_convert_pha_to_vtk(pha_path.encode(), vtk_path.encode())
     if st != OK:
         raise ScftError(st, lib.scft_last_error(None).decode())
+
+
+class Spline:
+    """Cubic interpolating spline (the reference's spline.c: spline, seval,
+    deriv, sinteg), coefficients from the library's scft_spline."""
+
+    def __init__(self, x, y, end1: int = 0, end2: int = 0, slope1: float = 0.0,
+                 slope2: float = 0.0):
+        self.lib = load_library()
+        self.x = np.ascontiguousarray(x, dtype=np.float64)
+        self.y = np.ascontiguousarray(y, dtype=np.float64)
+        n = self.n = len(self.x)
+        self.b, self.c, self.d = np.zeros(n), np.zeros(n), np.zeros(n)
+        flag = C.c_int()
+        st = self.lib.scft_spline(n, end1, end2, slope1, slope2, _dptr(self.x), _dptr(self.y),
+                                  _dptr(self.b), _dptr(self.c), _dptr(self.d), C.byref(flag))
+        if st != OK:
+            raise ScftError(st, "scft_spline")
+        self.iflag = flag.value
+        self.last = C.c_int(0)
+
+    def _args(self):
+        return _dptr(self.x), _dptr(self.y), _dptr(self.b), _dptr(self.c), _dptr(self.d)
+
+    def __call__(self, u: float) -> float:
+        x, y, b, c, d = self._args()
+        return self.lib.scft_spline_eval(self.n, u, x, y, b, c, d, C.byref(self.last))
+
+    def deriv(self, u: float) -> float:
+        x, _, b, c, d = self._args()
+        return self.lib.scft_spline_deriv(self.n, u, x, b, c, d, C.byref(self.last))
+
+    def integral(self, u: float) -> float:
+        x, y, b, c, d = self._args()
+        return self.lib.scft_spline_integral(self.n, u, x, y, b, c, d, C.byref(self.last))
+
+    def eval_device(self, u, mode: int = 0):
+        """Batched evaluation on the GPU: u a CUDA float64 tensor -> tensor
+        (mode 0 value, 1 derivative, 2 integral from x[0])."""
+        import torch
+        dev = u.device
+        coef = [torch.as_tensor(a, device=dev) for a in (self.x, self.y, self.b, self.c, self.d)]
+        out = torch.empty_like(u)
+        torch.cuda.synchronize(dev)
+        st = self.lib.scft_spline_eval_device(self.n, *[t.data_ptr() for t in coef], u.data_ptr(),
+                                              out.data_ptr(), u.numel(), mode, None)
+        torch.cuda.synchronize(dev)
+        if st != OK:
+            raise ScftError(st, "scft_spline_eval_device")
+        return out
 
 
 def _dptr(a: np.ndarray):

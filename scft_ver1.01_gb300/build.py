@@ -23,7 +23,11 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 
 SOURCES = ["capi.cu", "io.cpp", "compat.cpp", "k_line.cu", "k_fields.cu", "k_fast.cu",
-           "k_anderson.cu", "group.cu", "noalloc.cu", "adjoint.cu"]
+           "k_anderson.cu", "group.cu", "noalloc.cu", "adjoint.cu", "spline.cu"]
+# Per-file extra flags: the spline's host arithmetic keeps the reference's
+# rounding (no FMA contraction by the host compiler, which aarch64 gcc does by
+# default).
+EXTRA_FLAGS = {"spline.cu": ["-Xcompiler", "-ffp-contract=off"]}
 # Drop-in driver of the reference's struct API (init_scft -> fft_test ->
 # finalize_cufft), linked against the library: the reference's `scan` binary.
 DRIVER_SRC = "scft_main.cpp"
@@ -63,7 +67,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         obj = os.path.join(BUILD, src + ".o")
         objs.append(obj)
         if _stale(obj, [spath] + hdrs + [__file__]):
-            cmds.append([cc] + NVCC_FLAGS + ["-c", spath, "-o", obj])
+            cmds.append([cc] + NVCC_FLAGS + EXTRA_FLAGS.get(src, []) + ["-c", spath, "-o", obj])
 
     def run(cmd):
         if verbose:
