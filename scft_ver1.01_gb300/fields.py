@@ -52,11 +52,13 @@ def hexagonal(nx, ny, nz, lx, ly, lz, chiN, seed, batch=1, amp=0.2, noise=0.02):
     return wa, wb
 
 
-def mixture(nx, ny, nz, lx, ly, lz, chiN, seed, batch=1, amp=0.1, noise=0.02):
-    """Lamellar + gyroid mixture: chiN*amp*(cos(2 pi x/Lx) + g(r)) + N(0, noise)."""
+def mixture(nx, ny, nz, lx, ly, lz, chiN, seed, batch=1, amp=0.1, noise=0.02, periods=1):
+    """Lamellar + gyroid mixture: chiN*amp*(cos(X) + g(r)) + N(0, noise) with
+    X = 2 pi periods x / Lx (likewise Y, Z): `periods` unit cells per box."""
     rng = np.random.default_rng(seed)
     x, y, z = _coords(nx, ny, nz, lx, ly, lz)
-    X, Y, Z = 2 * np.pi * x / lx, 2 * np.pi * y / ly, 2 * np.pi * z / lz
+    k = 2 * np.pi * periods
+    X, Y, Z = k * x / lx, k * y / ly, k * z / lz
     g = np.sin(X) * np.cos(Y) + np.sin(Y) * np.cos(Z) + np.sin(Z) * np.cos(X)
     base = chiN * amp * (np.cos(X) + g)
     wa = base[None] + rng.normal(0.0, noise, (batch, nz, ny, nx))
