@@ -248,6 +248,12 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
                F_abs_diff=abs(fep[0, 0] - fe64[0, 0]),
                # phi and Q of the last getConc of each run (both converged)
                phiA_rel_diff=float(np.abs(phamx - pha64).max() / np.abs(pha64).max()),
+               # the same with the translation zero mode removed: a converged
+               # structure may sit shifted by a fraction of a voxel at the
+               # same F, so compare the moduli of the Fourier coefficients
+               phiA_spectrum_rel_diff=float(
+                   np.abs(np.abs(np.fft.rfftn(phamx[0])) - np.abs(np.fft.rfftn(pha64[0]))).max()
+                   / np.abs(np.fft.rfftn(pha64[0])).max()),
                Q_rel_diff=float(abs(Qmx[0] - Q64[0]) / abs(Q64[0])))
     return out
 

@@ -119,11 +119,9 @@ bool axis_ok(int n, bool allow_one) {
 // kernel, or one generic launch per set member.
 template <typename R>
 int launch_set(scft_ctx *ctx, const AxisPlan &ap, const scft::PassSet<R> &ps, cudaStream_t st) {
-  if constexpr (sizeof(R) == 4) {
-    if (ap.use_fast) {
-      CKL(scft::launch_fast_line(ap, ps, st));
-      return SCFT_OK;
-    }
+  if (ap.use_fast) {
+    CKL(scft::launch_fast_line(ap, ps, st));
+    return SCFT_OK;
   }
   for (int k = 0; k < ps.nset; ++k)
     CKL(scft::launch_line_filter<R>(ap, ps.in[k], ps.in_bs[k], ps.out[k], ps.out_bs[k],
@@ -668,8 +666,9 @@ void free_all(scft_ctx *ctx) {
 // replays after a warm-up, minimum taken); the fastest stays.  The fields are
 // whatever the context holds (timings do not depend on their values).
 int autotune(scft_ctx *ctx) {
-  bool has_fast_col = false;
-  for (size_t i = 1; i < ctx->passes.size(); ++i) has_fast_col |= ctx->passes[i].use_fast != 0;
+  bool has_fast_col = false;   // the persistent column kernel exists in FP32 only
+  for (size_t i = 1; i < ctx->passes.size(); ++i)
+    has_fast_col |= ctx->rbytes == 4 && ctx->passes[i].use_fast != 0;
   const bool can_xy = ctx->fuse_xy;
   const bool can_fs = (ctx->p.flags & SCFT_FLAG_NO_FUSED_STEPS) == 0 && ctx->rbytes == 4 &&
                       ctx->passes.size() == 3;
@@ -957,7 +956,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     if (tl < 1) tl = 1;
     if (tl > n_pairs) tl = n_pairs;
     ap.tl = tl;
-    ap.use_fast = (rb == 4 && scft::fast_line_supported(ap)) ? 1 : 0;
+    ap.use_fast = scft::fast_line_supported(ap, rb) ? 1 : 0;
     if (scft::line_filter_smem_bytes(ap, rb) > (size_t)scft::kLineSmemMax)
       return fail(SCFT_ERR_UNSUPPORTED, "line too long for shared memory");
     // twiddles exp(-2 pi i m / n); the gains are filled by upload_gains

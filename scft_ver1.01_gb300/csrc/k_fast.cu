@@ -24,197 +24,16 @@ namespace scft {
 namespace {
 
 // Shared memory of k_fast_line before its tables: the exchange buffer
-// (N x 32 complex), or the 64-row staging tile (pitch N+1) of the x pass.
-template <int N, bool XP> __host__ __device__ constexpr size_t fast_core_smem() {
-  return ((size_t)N * 32 * 8 > (XP ? (size_t)64 * (N + 1) * 4 : 0))
-             ? (size_t)N * 32 * 8
-             : (((size_t)64 * (N + 1) * 4 + 15) / 16) * 16;
-}
-
-// Column passes keep the Boltzmann-factor tile of their output (N rows x 64
-// floats) in shared memory after the twiddle/gain tables.
-template <int N, bool XP> __host__ __device__ constexpr size_t fast_wtile_off() {
-  return ((fast_core_smem<N, XP>() + (size_t)N * 12 + 15) / 16) * 16;
-}
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-template <int N, int P, bool XP>
-__global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<float> ps) {
-  constexpr int R1 = N / P;
-  constexpr int NT = P * 32;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  float2 *ex = reinterpret_cast<float2 *>(smem_raw);
-  const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
-  // blockIdx.z = set * batch + instance
-  const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
-  const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
-  const float *__restrict__ in = set ? ps.in[1] : ps.in[0];
-  float *__restrict__ out = set ? ps.out[1] : ps.out[0];
-  const float *__restrict__ pre = set ? ps.pre[1] : ps.pre[0];
-  const float *__restrict__ post = set ? ps.post[1] : ps.post[0];
-  const long long in_bs = set ? ps.in_bs[1] : ps.in_bs[0];
-  const long long out_bs = set ? ps.out_bs[1] : ps.out_bs[0];
-  const long long w_bs = ps.w_bs;
-  // The twiddle and gain tables go to shared memory first: they do not depend
-  // on the previous pass, so this overlaps its tail, and the FFT stages then
-  // read them with shared-memory broadcasts instead of dependent global loads.
-  float2 *s_tw = reinterpret_cast<float2 *>(smem_raw + fast_core_smem<N, XP>());
-  float *s_g = reinterpret_cast<float *>(s_tw + N);
-  for (int i = threadIdx.x; i < N; i += NT) {
-    s_tw[i] = __ldg(reinterpret_cast<const float2 *>(ap.twiddle) + i);
-    s_g[i] = __ldg(reinterpret_cast<const float *>(ap.gain) + i);
-  }
-  // Column passes with a post factor: the factor's tile does not depend on
-  // the previous pass either, so its cp.async copies are issued here too and
-  // land while the lines are loaded and filtered (the epilogue then reads
-  // shared memory instead of waiting on global loads).
-  float *s_wt = reinterpret_cast<float *>(smem_raw + fast_wtile_off<N, XP>());
-  if constexpr (!XP) {
-    if (post) {
-      const float *wt = post + b * w_bs + (long long)blockIdx.y * ap.s_outer +
-                        (long long)blockIdx.x * 64;
-      for (int c = threadIdx.x; c < N * 16; c += NT) {
-        const int row = c >> 4, part = c & 15;
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                         smem_addr(s_wt + row * 64 + part * 4)),
-                     "l"(wt + (long long)row * ap.s_n + part * 4)
-                     : "memory");
-      }
-      asm volatile("cp.async.commit_group;" ::: "memory");
-    }
-  }
-  // the input slice is the previous pass's output
-  pdl_wait();
-  pdl_release();
-  const float2 *tw = s_tw;
-  const float *gain = s_g;
-  float2 v[R1];
-  long long base;
-
-  if constexpr (XP) {
-    constexpr int PITCH = N + 1;
-    float *stg = reinterpret_cast<float *>(smem_raw);
-    base = (long long)blockIdx.x * 64 * N;  // 64 consecutive rows of N floats
-    const float *src = in + b * in_bs + base;
-    const float *wsrc = pre ? pre + b * w_bs + base : nullptr;
-#pragma unroll
-    for (int i = threadIdx.x; i < 64 * N; i += NT) {
-      const int r = i / N, c = i % N;
-      float x = __ldg(src + i);
-      if (wsrc) x *= __ldg(wsrc + i);
-      stg[r * PITCH + c] = x;
-    }
-    __syncthreads();
-    reg::static_for<0, R1>([&](auto j_) {
-      constexpr int j = decltype(j_)::value;
-      const int n = p + P * j;
-      v[j] = make_float2(stg[lane * PITCH + n], stg[(lane + 32) * PITCH + n]);
-    });
-    __syncthreads();
-  } else {
-    base = (long long)blockIdx.y * ap.s_outer + (long long)blockIdx.x * 64 + 2 * lane;
-    const float *src = in + b * in_bs + base;
-    reg::static_for<0, R1>([&](auto j_) {
-      constexpr int j = decltype(j_)::value;
-      v[j] = __ldg(reinterpret_cast<const float2 *>(src + (long long)(p + P * j) * ap.s_n));
-    });
-    if (pre) {
-      const float *ws = pre + b * w_bs + base;
-      reg::static_for<0, R1>([&](auto j_) {
-        constexpr int j = decltype(j_)::value;
-        const float2 w =
-            __ldg(reinterpret_cast<const float2 *>(ws + (long long)(p + P * j) * ap.s_n));
-        v[j].x *= w.x;
-        v[j].y *= w.y;
-      });
-    }
-    __syncthreads();   // the shared tables are complete
-  }
-
-  // ---- stage 1: DFT_R1 over j, twiddle, exchange
-  reg::dft<R1, false>(v);
-  reg::static_for<0, R1>([&](auto k_) {
-    constexpr int k1 = decltype(k_)::value;
-    if (k1 > 0) v[k1] = cmul(v[k1], tw[p * k1]);
-    ex[(k1 * P + p) * 32 + lane] = v[k1];
-  });
-  __syncthreads();
-
-  // ---- stage 2: DFT_P over p, gain, inverse DFT_P, conjugate twiddle
-  for (int k1 = p; k1 < R1; k1 += P) {
-    float2 u[P];
-    reg::static_for<0, P>([&](auto q_) {
-      constexpr int q = decltype(q_)::value;
-      u[q] = ex[(k1 * P + q) * 32 + lane];
-    });
-    reg::dft<P, false>(u);
-    reg::static_for<0, P>([&](auto k2_) {
-      constexpr int k2 = decltype(k2_)::value;
-      const float g = gain[k1 + R1 * k2];
-      u[k2].x *= g;
-      u[k2].y *= g;
-    });
-    reg::dft<P, true>(u);
-    reg::static_for<0, P>([&](auto q_) {
-      constexpr int q = decltype(q_)::value;
-      if (q > 0) u[q] = cmul(u[q], cconj(tw[q * k1]));
-      ex[(k1 * P + q) * 32 + lane] = u[q];
-    });
-  }
-  __syncthreads();
-
-  // ---- inverse stage 1
-  reg::static_for<0, R1>([&](auto k_) {
-    constexpr int k1 = decltype(k_)::value;
-    v[k1] = ex[(k1 * P + p) * 32 + lane];
-  });
-  reg::dft<R1, true>(v);
-
-  if constexpr (XP) {
-    constexpr int PITCH = N + 1;
-    float *stg = reinterpret_cast<float *>(smem_raw);
-    __syncthreads();  // every warp has read its exchange slots
-    reg::static_for<0, R1>([&](auto j_) {
-      constexpr int j = decltype(j_)::value;
-      const int n = p + P * j;
-      stg[lane * PITCH + n] = v[j].x;
-      stg[(lane + 32) * PITCH + n] = v[j].y;
-    });
-    __syncthreads();
-    float *dst = out + b * out_bs + base;
-    const float *wdst = post ? post + b * w_bs + base : nullptr;
-#pragma unroll 4
-    for (int i = threadIdx.x; i < 64 * N; i += NT) {
-      const int r = i / N, c = i % N;
-      float x = stg[r * PITCH + c];
-      if (wdst) x *= __ldg(wdst + i);
-      dst[i] = x;
-    }
-  } else {
-    float *dst = out + b * out_bs + base;
-    if (post) {
-      asm volatile("cp.async.wait_all;" ::: "memory");
-      __syncthreads();   // every thread's tile copies are visible
-    }
-    reg::static_for<0, R1>([&](auto j_) {
-      constexpr int j = decltype(j_)::value;
-      const long long off = (long long)(p + P * j) * ap.s_n;
-      float2 r = v[j];
-      if (post) {
-        const float2 w = reinterpret_cast<const float2 *>(s_wt)[(p + P * j) * 32 + lane];
-        r.x *= w.x;
-        r.y *= w.y;
-      }
-      *reinterpret_cast<float2 *>(dst + off) = r;
-    });
-  }
+// (N x 32 complex), or the 64-row staging tile (pitch N+1) of the x pass,
+// for real type T (float or double).
+template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_core_smem() {
+  return ((size_t)N * 32 * 2 * sizeof(T) > (XP ? (size_t)64 * (N + 1) * sizeof(T) : 0))
+             ? (size_t)N * 32 * 2 * sizeof(T)
+             : (((size_t)64 * (N + 1) * sizeof(T) + 15) / 16) * 16;
 }
 
 // ------------------------------------------------------------------------
-// The four-step filter core shared by the pipelined kernel: v[j] holds
+// The four-step filter core (FP32 or FP64 complex C, real T): v[j] holds
 // element p + P*j of complex column `lane` on entry and the filtered values
 // on exit.  `after_first_sync` runs once every warp has written its stage-1
 // exchange slots (so every warp has finished reading its inputs).
@@ -226,10 +45,9 @@ __device__ __forceinline__ void group_sync(int bar_id, int nthreads) {
   else asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(nthreads) : "memory");
 }
 
-template <int N, int P, typename F>
-__device__ __forceinline__ void four_step(float2 (&v)[N / P], float2 *ex, const float2 *tw,
-                                          const float *gain, int p, int lane, int bar_id,
-                                          F &&after_first_sync) {
+template <int N, int P, typename C, typename T, typename F>
+__device__ __forceinline__ void four_step(C (&v)[N / P], C *ex, const C *tw, const T *gain, int p,
+                                          int lane, int bar_id, F &&after_first_sync) {
   constexpr int R1 = N / P;
   reg::dft<R1, false>(v);
   reg::static_for<0, R1>([&](auto k_) {
@@ -240,7 +58,7 @@ __device__ __forceinline__ void four_step(float2 (&v)[N / P], float2 *ex, const 
   group_sync(bar_id, P * 32);
   after_first_sync();
   for (int k1 = p; k1 < R1; k1 += P) {
-    float2 u[P];
+    C u[P];
     reg::static_for<0, P>([&](auto q_) {
       constexpr int q = decltype(q_)::value;
       u[q] = ex[(k1 * P + q) * 32 + lane];
@@ -248,7 +66,7 @@ __device__ __forceinline__ void four_step(float2 (&v)[N / P], float2 *ex, const 
     reg::dft<P, false>(u);
     reg::static_for<0, P>([&](auto k2_) {
       constexpr int k2 = decltype(k2_)::value;
-      const float g = gain[k1 + R1 * k2];
+      const T g = gain[k1 + R1 * k2];
       u[k2].x *= g;
       u[k2].y *= g;
     });
@@ -266,6 +84,150 @@ __device__ __forceinline__ void four_step(float2 (&v)[N / P], float2 *ex, const 
   });
   reg::dft<R1, true>(v);
   group_sync(bar_id, P * 32);   // the exchange buffer is free again
+}
+
+// Column passes keep the Boltzmann-factor tile of their output (N rows x 64
+// floats) in shared memory after the twiddle/gain tables.
+template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_wtile_off() {
+  return ((fast_core_smem<T, N, XP>() + (size_t)N * 3 * sizeof(T) + 15) / 16) * 16;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+template <typename T, int N, int P, bool XP>
+__global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps) {
+  using C = typename cplx<T>::type;
+  constexpr int R1 = N / P;
+  constexpr int NT = P * 32;
+  constexpr int EPC = 16 / (int)sizeof(T);   // reals per 16-byte copy
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  C *ex = reinterpret_cast<C *>(smem_raw);
+  const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
+  // blockIdx.z = set * batch + instance
+  const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
+  const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
+  const T *__restrict__ in = set ? ps.in[1] : ps.in[0];
+  T *__restrict__ out = set ? ps.out[1] : ps.out[0];
+  const T *__restrict__ pre = set ? ps.pre[1] : ps.pre[0];
+  const T *__restrict__ post = set ? ps.post[1] : ps.post[0];
+  const long long in_bs = set ? ps.in_bs[1] : ps.in_bs[0];
+  const long long out_bs = set ? ps.out_bs[1] : ps.out_bs[0];
+  const long long w_bs = ps.w_bs;
+  // The twiddle and gain tables go to shared memory first: they do not depend
+  // on the previous pass, so this overlaps its tail, and the FFT stages then
+  // read them with shared-memory broadcasts instead of dependent global loads.
+  C *s_tw = reinterpret_cast<C *>(smem_raw + fast_core_smem<T, N, XP>());
+  T *s_g = reinterpret_cast<T *>(s_tw + N);
+  for (int i = threadIdx.x; i < N; i += NT) {
+    s_tw[i] = __ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
+    s_g[i] = __ldg(reinterpret_cast<const T *>(ap.gain) + i);
+  }
+  // Column passes with a post factor: the factor's tile does not depend on
+  // the previous pass either, so its cp.async copies are issued here too and
+  // land while the lines are loaded and filtered (the epilogue then reads
+  // shared memory instead of waiting on global loads).
+  T *s_wt = reinterpret_cast<T *>(smem_raw + fast_wtile_off<T, N, XP>());
+  if constexpr (!XP) {
+    if (post) {
+      constexpr int CPR = 64 / EPC;   // 16-byte copies per tile row of 64 reals
+      const T *wt = post + b * w_bs + (long long)blockIdx.y * ap.s_outer +
+                    (long long)blockIdx.x * 64;
+      for (int c = threadIdx.x; c < N * CPR; c += NT) {
+        const int row = c / CPR, part = c % CPR;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                         smem_addr(s_wt + row * 64 + part * EPC)),
+                     "l"(wt + (long long)row * ap.s_n + part * EPC)
+                     : "memory");
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+  }
+  // the input slice is the previous pass's output
+  pdl_wait();
+  pdl_release();
+  C v[R1];
+  long long base;
+
+  if constexpr (XP) {
+    constexpr int PITCH = N + 1;
+    T *stg = reinterpret_cast<T *>(smem_raw);
+    base = (long long)blockIdx.x * 64 * N;  // 64 consecutive rows of N reals
+    const T *src = in + b * in_bs + base;
+    const T *wsrc = pre ? pre + b * w_bs + base : nullptr;
+#pragma unroll
+    for (int i = threadIdx.x; i < 64 * N; i += NT) {
+      const int r = i / N, c = i % N;
+      T x = __ldg(src + i);
+      if (wsrc) x *= __ldg(wsrc + i);
+      stg[r * PITCH + c] = x;
+    }
+    __syncthreads();
+    reg::static_for<0, R1>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      const int n = p + P * j;
+      v[j] = mkc<C, T>(stg[lane * PITCH + n], stg[(lane + 32) * PITCH + n]);
+    });
+    __syncthreads();
+  } else {
+    base = (long long)blockIdx.y * ap.s_outer + (long long)blockIdx.x * 64 + 2 * lane;
+    const T *src = in + b * in_bs + base;
+    reg::static_for<0, R1>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      v[j] = __ldg(reinterpret_cast<const C *>(src + (long long)(p + P * j) * ap.s_n));
+    });
+    if (pre) {
+      const T *ws = pre + b * w_bs + base;
+      reg::static_for<0, R1>([&](auto j_) {
+        constexpr int j = decltype(j_)::value;
+        const C w = __ldg(reinterpret_cast<const C *>(ws + (long long)(p + P * j) * ap.s_n));
+        v[j].x *= w.x;
+        v[j].y *= w.y;
+      });
+    }
+    __syncthreads();   // the shared tables are complete
+  }
+
+  four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
+
+  if constexpr (XP) {
+    constexpr int PITCH = N + 1;
+    T *stg = reinterpret_cast<T *>(smem_raw);
+    reg::static_for<0, R1>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      const int n = p + P * j;
+      stg[lane * PITCH + n] = v[j].x;
+      stg[(lane + 32) * PITCH + n] = v[j].y;
+    });
+    __syncthreads();
+    T *dst = out + b * out_bs + base;
+    const T *wdst = post ? post + b * w_bs + base : nullptr;
+#pragma unroll 4
+    for (int i = threadIdx.x; i < 64 * N; i += NT) {
+      const int r = i / N, c = i % N;
+      T x = stg[r * PITCH + c];
+      if (wdst) x *= __ldg(wdst + i);
+      dst[i] = x;
+    }
+  } else {
+    T *dst = out + b * out_bs + base;
+    if (post) {
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      __syncthreads();   // every thread's tile copies are visible
+    }
+    reg::static_for<0, R1>([&](auto j_) {
+      constexpr int j = decltype(j_)::value;
+      const long long off = (long long)(p + P * j) * ap.s_n;
+      C r = v[j];
+      if (post) {
+        const C w = reinterpret_cast<const C *>(s_wt)[(p + P * j) * 32 + lane];
+        r.x *= w.x;
+        r.y *= w.y;
+      }
+      *reinterpret_cast<C *>(dst + off) = r;
+    });
+  }
 }
 
 // ---- mbarrier / bulk-copy helpers (bounded waits) ------------------------
@@ -550,13 +512,13 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<float> ps) {
   float *__restrict__ out = ps.out[set];
   float *__restrict__ qo = ps.qout[set];
   const float *__restrict__ w = ps.post[set];
-  float2 *s_tw = reinterpret_cast<float2 *>(smem_raw + fast_core_smem<N, false>());
+  float2 *s_tw = reinterpret_cast<float2 *>(smem_raw + fast_core_smem<float, N, false>());
   float *s_g = reinterpret_cast<float *>(s_tw + N);
   for (int i = threadIdx.x; i < N; i += NT) {
     s_tw[i] = __ldg(reinterpret_cast<const float2 *>(ap.twiddle) + i);
     s_g[i] = __ldg(reinterpret_cast<const float *>(ap.gain) + i);
   }
-  float *s_wt = reinterpret_cast<float *>(smem_raw + fast_wtile_off<N, false>());
+  float *s_wt = reinterpret_cast<float *>(smem_raw + fast_wtile_off<float, N, false>());
   const long long tile = (long long)blockIdx.y * ap.s_outer + (long long)blockIdx.x * 64;
   {
     const float *wt = w + b * ps.w_bs + tile;
@@ -608,7 +570,7 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<float> ps) {
 // k_fast_line: 64 rows per CTA staged through shared memory, pitch N+1).
 // The factor's tile (64 rows x N, contiguous in memory) is copied with
 // cp.async before the dependency wait.
-template <int N> constexpr size_t xx_wtile_off() { return fast_wtile_off<N, true>(); }
+template <int N> constexpr size_t xx_wtile_off() { return fast_wtile_off<float, N, true>(); }
 template <int N> constexpr size_t xx_smem() { return xx_wtile_off<N>() + (size_t)64 * N * 4; }
 
 template <int N, int P>
@@ -622,7 +584,7 @@ __global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<float> ps) {
   const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
   const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
   const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
-  float2 *s_tw = reinterpret_cast<float2 *>(smem_raw + fast_core_smem<N, true>());
+  float2 *s_tw = reinterpret_cast<float2 *>(smem_raw + fast_core_smem<float, N, true>());
   float *s_g = reinterpret_cast<float *>(s_tw + N);
   for (int i = threadIdx.x; i < N; i += NT) {
     s_tw[i] = __ldg(reinterpret_cast<const float2 *>(ap.twiddle) + i);
@@ -805,26 +767,29 @@ __global__ void __launch_bounds__(256 * G, 1)
   }
 }
 
-template <int N, int P, bool XP> size_t fast_smem() {
-  return XP ? fast_core_smem<N, XP>() + (size_t)N * (sizeof(float2) + sizeof(float))
-            : fast_wtile_off<N, XP>() + (size_t)N * 64 * sizeof(float);
+template <typename T, int N, int P, bool XP> size_t fast_smem() {
+  return XP ? fast_core_smem<T, N, XP>() + (size_t)N * 3 * sizeof(T)
+            : fast_wtile_off<T, N, XP>() + (size_t)N * 64 * sizeof(T);
 }
 
-template <int N, int P, bool XP>
-cudaError_t launch_one(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
+template <typename T, int N, int P, bool XP>
+cudaError_t launch_one(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
   dim3 grid(ap.n_real / 64, XP ? 1 : ap.n_outer, ps.nset * ps.batch);
-  return launch_pdl(k_fast_line<N, P, XP>, grid, dim3(P * 32), fast_smem<N, P, XP>(), st, ap, ps);
+  return launch_pdl(k_fast_line<T, N, P, XP>, grid, dim3(P * 32), fast_smem<T, N, P, XP>(), st,
+                    ap, ps);
 }
 
-template <int N, int P, bool XP> cudaError_t prep_one() {
-  return cudaFuncSetAttribute(k_fast_line<N, P, XP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)fast_smem<N, P, XP>());
+template <typename T, int N, int P, bool XP> cudaError_t prep_one() {
+  return cudaFuncSetAttribute(k_fast_line<T, N, P, XP>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)fast_smem<T, N, P, XP>());
 }
 
 }  // namespace
 
-bool fast_line_supported(const AxisPlan &ap) {
-  if (ap.n != 32 && ap.n != 64 && ap.n != 128 && ap.n != 256) return false;
+bool fast_line_supported(const AxisPlan &ap, size_t real_bytes) {
+  // FP64 lines stop at 128 points (256 would not fit the registers)
+  if (ap.n != 32 && ap.n != 64 && ap.n != 128 && !(ap.n == 256 && real_bytes == 4)) return false;
   return ap.n_real % 64 == 0;
 }
 
@@ -899,12 +864,12 @@ cudaError_t launch_xx_t(const AxisPlan &ap, const PassSet<float> &ps, cudaStream
 }
 template <int N, int P> cudaError_t prep_zz() {
   return cudaFuncSetAttribute(k_zz<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)fast_smem<N, P, false>());
+                              (int)fast_smem<float, N, P, false>());
 }
 template <int N, int P>
 cudaError_t launch_zz_t(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
   dim3 grid(ap.n_real / 64, ap.n_outer, ps.nset * ps.batch);
-  return launch_pdl(k_zz<N, P>, grid, dim3(P * 32), fast_smem<N, P, false>(), st, ap, ps);
+  return launch_pdl(k_zz<N, P>, grid, dim3(P * 32), fast_smem<float, N, P, false>(), st, ap, ps);
 }
 // 16-byte cp.async tiles and float2 lines: refuse misaligned buffers
 bool fused_aligned(const PassSet<float> &ps) {
@@ -969,13 +934,16 @@ cudaError_t launch_xy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<fl
 
 cudaError_t fast_line_prepare() {
   cudaError_t e = cudaSuccess;
-#define PREP(N, P)                                              \
-  if ((e = prep_one<N, P, false>()) != cudaSuccess) return e;  \
-  if ((e = prep_one<N, P, true>()) != cudaSuccess) return e;
-  PREP(32, 4)
-  PREP(64, 8)
-  PREP(128, 8)
-  PREP(256, 16)
+#define PREP(T, N, P)                                              \
+  if ((e = prep_one<T, N, P, false>()) != cudaSuccess) return e;  \
+  if ((e = prep_one<T, N, P, true>()) != cudaSuccess) return e;
+  PREP(float, 32, 4)
+  PREP(float, 64, 8)
+  PREP(float, 128, 8)
+  PREP(float, 256, 16)
+  PREP(double, 32, 4)
+  PREP(double, 64, 8)
+  PREP(double, 128, 8)
 #undef PREP
   int dev = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
@@ -1024,12 +992,39 @@ cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaS
     }
   }
   switch (ap.n) {
-    case 32: return xp ? launch_one<32, 4, true>(ap, ps, st) : launch_one<32, 4, false>(ap, ps, st);
-    case 64: return xp ? launch_one<64, 8, true>(ap, ps, st) : launch_one<64, 8, false>(ap, ps, st);
+    case 32:
+      return xp ? launch_one<float, 32, 4, true>(ap, ps, st)
+                : launch_one<float, 32, 4, false>(ap, ps, st);
+    case 64:
+      return xp ? launch_one<float, 64, 8, true>(ap, ps, st)
+                : launch_one<float, 64, 8, false>(ap, ps, st);
     case 128:
-      return xp ? launch_one<128, 8, true>(ap, ps, st) : launch_one<128, 8, false>(ap, ps, st);
+      return xp ? launch_one<float, 128, 8, true>(ap, ps, st)
+                : launch_one<float, 128, 8, false>(ap, ps, st);
     case 256:
-      return xp ? launch_one<256, 16, true>(ap, ps, st) : launch_one<256, 16, false>(ap, ps, st);
+      return xp ? launch_one<float, 256, 16, true>(ap, ps, st)
+                : launch_one<float, 256, 16, false>(ap, ps, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st) {
+  if (ps.nset < 1 || ps.nset > kMaxSet) return cudaErrorInvalidValue;
+  for (int k = 0; k < ps.nset; ++k)
+    if ((reinterpret_cast<uintptr_t>(ps.post[k]) | reinterpret_cast<uintptr_t>(ps.pre[k]) |
+         reinterpret_cast<uintptr_t>(ps.in[k]) | reinterpret_cast<uintptr_t>(ps.out[k])) & 15)
+      return cudaErrorMisalignedAddress;
+  const bool xp = ap.n_fast != 0;
+  switch (ap.n) {
+    case 32:
+      return xp ? launch_one<double, 32, 4, true>(ap, ps, st)
+                : launch_one<double, 32, 4, false>(ap, ps, st);
+    case 64:
+      return xp ? launch_one<double, 64, 8, true>(ap, ps, st)
+                : launch_one<double, 64, 8, false>(ap, ps, st);
+    case 128:
+      return xp ? launch_one<double, 128, 8, true>(ap, ps, st)
+                : launch_one<double, 128, 8, false>(ap, ps, st);
     default: return cudaErrorInvalidValue;
   }
 }

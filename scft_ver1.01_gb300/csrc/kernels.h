@@ -47,15 +47,16 @@ template <typename R> struct PassSet {
   long long qout_bs[kMaxSet];
 };
 
-// Register-resident FP32 pass (k_fast.cu): n in {32, 64, 128, 256} and
-// n_real a multiple of 64.
-bool fast_line_supported(const AxisPlan &ap);
+// Register-resident pass (k_fast.cu): n in {32, 64, 128, 256} (FP32) or
+// {32, 64, 128} (FP64), and n_real a multiple of 64.
+bool fast_line_supported(const AxisPlan &ap, size_t real_bytes = 4);
 // Fused x+y pass over whole z-planes (k_fast.cu): Nx, Ny in {64, 128}.
 bool xy_fusable(const AxisPlan &apx, const AxisPlan &apy);
 cudaError_t launch_xy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
                       cudaStream_t st);
 cudaError_t fast_line_prepare();
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
+cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st);
 // Fused step pairs.  The axis filters commute, so consecutive contour steps
 // can run their passes in alternating order (x+y then z, z then x+y); the
 // end of one step and the start of the next are then the same pass type and
