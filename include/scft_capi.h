@@ -121,6 +121,13 @@ int scft_set_field(scft_ctx *ctx, int field, const double *src);
 /* Device -> host copy of one field; dst holds batch*M doubles. */
 int scft_get_field(scft_ctx *ctx, int field, double *dst);
 
+/* Failure-detection self-test (no reference counterpart): runs the bounded
+ * mbarrier wait of the pipelined kernels on a barrier nothing arrives at, for
+ * `seconds` (at most 10) of SM clock, on `device`.  *timed_out = 1 when the
+ * wait gave up and reported through the device error word (the kernel returns;
+ * nothing traps or hangs).  Returns SCFT_OK while the device stays usable. */
+int scft_selftest_bounded_wait(int device, double seconds, int *timed_out);
+
 /* Zero-copy access (no reference counterpart; the reference hands out its
  * per-GPU device pointers through CUFFT_INFO, struct.h:94-121): the device
  * address of a field ([batch][M] FP64 on the context's device), valid until

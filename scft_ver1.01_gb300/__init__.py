@@ -42,7 +42,7 @@ EXPORTS = [
     "scft_get_schedule", "scft_write_vtk", "scft_convert_pha_to_vtk", "scft_set_target",
     "scft_phi_w_constrained", "scft_set_box", "scft_stress", "scft_adjoint",
     "scft_adjoint_checkpoints", "scft_relax_cell", "scft_get_box", "scft_field_device_ptr",
-    "scft_get_stream", "scft_copy_q_reference_layout", "scft_spline", "scft_spline_eval",
+    "scft_get_stream", "scft_copy_q_reference_layout", "scft_selftest_bounded_wait", "scft_spline", "scft_spline_eval",
     "scft_spline_deriv", "scft_spline_integral", "scft_spline_eval_device",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
@@ -133,6 +133,7 @@ def load_library(path: str | None = None):
         "scft_field_device_ptr": (C.c_int, [vp, C.c_int, C.POINTER(dp)]),
         "scft_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
         "scft_copy_q_reference_layout": (C.c_int, [vp, C.c_int, vp]),
+        "scft_selftest_bounded_wait": (C.c_int, [C.c_int, C.c_double, C.POINTER(C.c_int)]),
         "scft_spline": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp,
                                   dp, dp, C.POINTER(C.c_int)]),
         "scft_spline_eval": (C.c_double, [C.c_int, C.c_double, dp, dp, dp, dp, dp,

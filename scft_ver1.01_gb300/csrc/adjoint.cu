@@ -567,6 +567,7 @@ int scft_adjoint(scft_ctx *ctx, const double *pha_bar, const double *phb_bar,
   const int N = ctx->NsA + ctx->dNsB;
   if (N < 1) return scft_fail(ctx, SCFT_ERR_UNSUPPORTED, "adjoint needs at least one step");
   if (checkpoint_every < 0) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad checkpoint interval");
+  NvtxRange range("scft adjoint");
   int K = checkpoint_every ? checkpoint_every : (int)ceil(sqrt((double)N));
   if (K > N) K = N;
   CK(cudaSetDevice(ctx->p.device));
@@ -594,6 +595,7 @@ int scft_stress(scft_ctx *ctx, double *dF_dL) {
     return scft_fail(ctx, SCFT_ERR_INVALID_ARG,
                      "no getConc at the current box: call scft_get_conc first");
   CK(cudaSetDevice(ctx->p.device));
+  NvtxRange range("scft stress");
   if (!ctx->adj) ctx->adj = new AdjointState();
   AdjointState &A = *ctx->adj;
   if (!A.smem) {

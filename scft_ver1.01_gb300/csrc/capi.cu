@@ -405,6 +405,7 @@ int march_phase(scft_ctx *ctx, cudaStream_t st) {
 // and step counts of a context never change), so one launch replays the
 // ~3*(NsA+dNsB) kernels of the phase.
 int march_phase_graph(scft_ctx *ctx) {
+  NvtxRange range("scft march phase");
   if (!ctx->use_graph || ctx->capturing) return march_phase(ctx, ctx->st);
   if (!ctx->march_exec) {
     const long long l0 = ctx->launches;
@@ -522,6 +523,7 @@ int q_and_phi(scft_ctx *ctx) {
 // (initilize_wdz, :450, once per field instead of once per march), the march
 // phase, then Q and the contour sums.
 int get_conc(scft_ctx *ctx) {
+  NvtxRange range("scft getConc");
   int rc;
   if ((rc = average(ctx, ctx->wa))) return rc;                                 // :71
   if ((rc = boltzmann(ctx, SCFT_FIELD_WA, ctx->st))) return rc;
@@ -539,6 +541,7 @@ int get_conc(scft_ctx *ctx) {
 // extends the FP64 Gram matrix by one row, solves the small least-squares
 // problem on the device and applies the mixed step.  No host round trip.
 int mix(scft_ctx *ctx) {
+  NvtxRange range("scft field update");
   const long long M = ctx->M;
   const int B = ctx->batch;
   if (ctx->p.mixing == SCFT_MIX_CONSTRAINED || ctx->p.mixing == SCFT_MIX_CONSTRAINED_EX) {
@@ -1209,6 +1212,29 @@ int scft_copy_q_reference_layout(scft_ctx *ctx, int q, double *dst_device) {
   return SCFT_OK;
 }
 
+int scft_selftest_bounded_wait(int device, double seconds, int *timed_out) {
+  scft_ctx *ctx = nullptr;   // errors go to the create-time message
+  if (!timed_out || !(seconds > 0) || seconds > 10)
+    return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "timed_out null or seconds not in (0, 10]");
+  *timed_out = 0;
+  int clk_khz = 0;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&clk_khz, cudaDevAttrClockRate, device) != cudaSuccess)
+    return scft_fail(nullptr, SCFT_ERR_NO_DEVICE, "no such device");
+  unsigned *err = nullptr;
+  CK(cudaMalloc(&err, sizeof(unsigned)));
+  unsigned h = 0;
+  cudaError_t e = cudaMemset(err, 0, sizeof(unsigned));
+  if (e == cudaSuccess)
+    e = scft::launch_wait_selftest(err, (long long)(seconds * clk_khz * 1e3), nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&h, err, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(err);
+  if (e != cudaSuccess) return scft_fail(nullptr, SCFT_ERR_CUDA, cudaGetErrorString(e));
+  *timed_out = (h & 4u) != 0;
+  return SCFT_OK;
+}
+
 int scft_field_device_ptr(scft_ctx *ctx, int field, double **dptr) {
   if (!ctx || !dptr) return SCFT_ERR_INVALID_ARG;
   double *p = field_ptr(ctx, field);
@@ -1256,6 +1282,7 @@ int scft_get_residual(scft_ctx *ctx, double *err_max, double *err_rms) {
 
 int scft_converge(scft_ctx *ctx, double tol, int max_it, int *iters, double *out5) {
   if (!ctx || max_it < 0 || !(tol > 0)) return SCFT_ERR_INVALID_ARG;
+  NvtxRange range("scft converge");
   std::vector<double> e(ctx->batch);
   int it = 0;
   while (it < max_it) {

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <string>
 #include <vector>
@@ -69,6 +70,14 @@ struct scft_ctx {
   std::vector<cudaEvent_t> prof_events;   // pairs, grown on demand
   size_t prof_used = 0;
   double prof_point_steps = 0.0;
+};
+
+// NVTX range for profilers (a no-op unless a tool is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
 };
 
 // Set ctx->err and return status.

@@ -252,8 +252,10 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
-// Wait for phase `parity` of `bar`, for at most ~1 s of SM clock; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+// Wait for phase `parity` of `bar`, for at most `limit` SM clocks (default
+// ~1 s); false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity,
+                                          long long limit = 2000000000LL) {
   const long long t0 = clock64();
   while (true) {
     unsigned done;
@@ -264,8 +266,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
         : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     if (done) return true;
-    if (clock64() - t0 > 2000000000LL) return false;
+    if (clock64() - t0 > limit) return false;
   }
+}
+
+// Self-test of the bounded wait: an mbarrier that nothing ever arrives at is
+// waited on for `limit` clocks; the timeout must set the error word and the
+// kernel must return (nothing traps or hangs).
+__global__ void k_wait_selftest(unsigned *err, long long limit) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (threadIdx.x == 0 && !mbar_wait(&bar, 0, limit)) atomicOr(err, 4u);
+  __syncthreads();
 }
 
 // Persistent, pipelined column pass (lines along y or z).  Each CTA loops over
@@ -892,6 +905,11 @@ cudaError_t launch_xx(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t
     case 256: return launch_xx_t<256, 16>(ap, ps, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_wait_selftest(unsigned *err, long long limit, cudaStream_t st) {
+  k_wait_selftest<<<1, 32, 0, st>>>(err, limit);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_zz(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {

@@ -55,6 +55,8 @@ bool xy_fusable(const AxisPlan &apx, const AxisPlan &apy);
 cudaError_t launch_xy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
                       cudaStream_t st);
 cudaError_t fast_line_prepare();
+// bounded-wait self-test: sets bit 4 of *err after `limit` clocks
+cudaError_t launch_wait_selftest(unsigned *err, long long limit, cudaStream_t st);
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st);
 // Fused step pairs.  The axis filters commute, so consecutive contour steps
