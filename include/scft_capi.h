@@ -107,8 +107,9 @@ int scft_create(const scft_params *p, scft_ctx **out);
 /* Replaces finalize_cufft (init_cuda.cu:551-628).  NULL is ignored. */
 void scft_destroy(scft_ctx *ctx);
 
-/* Message of the last failure on ctx (or of the last failed scft_create
- * when ctx is NULL).  Never NULL. */
+/* Message of the last failure on ctx (or, when ctx is NULL, of the calling
+ * host thread's last failed call without a context, e.g. scft_create).
+ * Never NULL. */
 const char *scft_last_error(const scft_ctx *ctx);
 const char *scft_strerror(int status);
 

@@ -18,7 +18,8 @@ namespace {
 // struct.h:11 -- the reference's value of pi, used for the wave numbers.
 constexpr double kPiRef = 3.1415926535;
 
-std::string g_create_err = "no error";
+// per host thread: contexts may be created from several threads at once
+thread_local std::string g_create_err = "no error";
 
 #define CK(call)                                                                        \
   do {                                                                                  \

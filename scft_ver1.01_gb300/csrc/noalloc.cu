@@ -44,7 +44,7 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) float g_noalloc_scratch[2 * kNoAllocMaxPoints + kTableFloats];
 
 float *g_scratch_dev[kMaxDevices] = {nullptr};   // device address of the array, per device
-std::string g_noalloc_err = "no error";
+thread_local std::string g_noalloc_err = "no error";   // per host thread
 
 int fail(int st, const std::string &m) {
   g_noalloc_err = m;
