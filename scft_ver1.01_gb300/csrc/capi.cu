@@ -882,10 +882,14 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   ctx->use_graph = (p.flags & SCFT_FLAG_NO_GRAPH) == 0;
   ctx->use_pipe = (p.flags & SCFT_FLAG_PIPE) != 0;
   // Two forked chains beat shared lockstep launches once a pass fills the GPU
-  // (measured: +16% at 128^3, +9% at 256^3, -8% at 64^3).
+  // (measured, FP32 unfused: +16% at 128^3, +9% at 256^3, -8% at 64^3; FP64:
+  // 25.2 against 32.1 ms per iteration at 64^3, even at 128^3).  With fused
+  // step pairs they win at every size (below).
+  const long long pts = (long long)p.nx * p.ny * p.nz * p.batch;
   ctx->two_streams = (p.flags & SCFT_FLAG_TWO_STREAMS) != 0 ||
-                     (p.flags & SCFT_FLAG_LOCKSTEP) == 0 &&
-                         (long long)p.nx * p.ny * p.nz * p.batch >= (1LL << 20);
+                     ((p.flags & SCFT_FLAG_LOCKSTEP) == 0 &&
+                      (pts >= (1LL << 20) ||
+                       (p.precision == SCFT_PREC_FP64 && pts >= (1LL << 18))));
   if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
