@@ -244,27 +244,27 @@ int run_chains(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int nch
 // end of one step with the start of the next, two launches per step instead
 // of three.
 bool fused_possible(const scft_ctx *ctx) {
-  if (!ctx->fuse_steps || ctx->rbytes != 4 || ctx->passes.size() != 3) return false;
-  if (ctx->fuse_xy) return ctx->passes[2].use_fast != 0;
+  if (!ctx->fuse_steps || ctx->passes.size() != 3) return false;
+  if (ctx->fuse_xy) return ctx->rbytes == 4 && ctx->passes[2].use_fast != 0;
   return ctx->passes[0].use_fast && ctx->passes[1].use_fast && ctx->passes[2].use_fast;
 }
 
+template <typename R>
 int run_chain_fused_axes(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t st, int cidx) {
   const long long M = ctx->M;
-  float *tmp[2] = {static_cast<float *>(ctx->tmp[2 * cidx]),
-                   static_cast<float *>(ctx->tmp[2 * cidx + 1])};
+  R *tmp[2] = {static_cast<R *>(ctx->tmp[2 * cidx]), static_cast<R *>(ctx->tmp[2 * cidx + 1])};
   const AxisPlan &apx = ctx->passes[0], &apy = ctx->passes[1], &apz = ctx->passes[2];
   for (int k = 0; k < nseg; ++k) {
     const Seg &sg = segs[k];
-    int rc = seg_boundary<float>(ctx, sg, st);
+    int rc = seg_boundary<R>(ctx, sg, st);
     if (rc) return rc;
     if (sg.ns == 0) continue;
-    float *q = static_cast<float *>(ctx->q[sg.qi]);
+    R *q = static_cast<R *>(ctx->q[sg.qi]);
     const long long qbs = (long long)(ctx->q_ns[sg.qi] + 1) * M;
-    const float *W = static_cast<const float *>(ctx->W[sg.wf]);
+    const R *W = static_cast<const R *>(ctx->W[sg.wf]);
     auto slice = [&](int it) { return q + (long long)(sg.sign > 0 ? it : sg.ns - it) * M; };
-    scft::PassSet<float> ps;
-    auto reset = [&](const float *in, long long in_bs, float *out, long long out_bs) {
+    scft::PassSet<R> ps;
+    auto reset = [&](const R *in, long long in_bs, R *out, long long out_bs) {
       memset(&ps, 0, sizeof(ps));
       ps.nset = 1;
       ps.batch = ctx->batch;
@@ -277,9 +277,9 @@ int run_chain_fused_axes(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t 
     // step 1: x with the pre factor, then y; tmp[0] holds the state between steps
     reset(slice(0), qbs, tmp[1], M);
     ps.pre[0] = W;
-    if ((rc = launch_set<float>(ctx, apx, ps, st))) return rc;
+    if ((rc = launch_set<R>(ctx, apx, ps, st))) return rc;
     reset(tmp[1], M, tmp[0], M);
-    if ((rc = launch_set<float>(ctx, apy, ps, st))) return rc;
+    if ((rc = launch_set<R>(ctx, apy, ps, st))) return rc;
     for (int it = 2; it <= sg.ns; ++it) {
       // finish step it-1 (z when it was odd, x when even) and start step it
       reset(tmp[0], M, tmp[1], M);
@@ -289,17 +289,19 @@ int run_chain_fused_axes(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t 
       if ((it - 1) & 1) CKL(scft::launch_zz(apz, ps, st));
       else CKL(scft::launch_xx(apx, ps, st));
       reset(tmp[1], M, tmp[0], M);
-      if ((rc = launch_set<float>(ctx, apy, ps, st))) return rc;
+      if ((rc = launch_set<R>(ctx, apy, ps, st))) return rc;
     }
     reset(tmp[0], M, slice(sg.ns), qbs);
     ps.post[0] = W;
-    if ((rc = launch_set<float>(ctx, (sg.ns & 1) ? apz : apx, ps, st))) return rc;
+    if ((rc = launch_set<R>(ctx, (sg.ns & 1) ? apz : apx, ps, st))) return rc;
   }
   return SCFT_OK;
 }
 
 int run_chain_fused(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t st, int cidx) {
-  if (!ctx->fuse_xy) return run_chain_fused_axes(ctx, segs, nseg, st, cidx);
+  if (!ctx->fuse_xy)
+    return ctx->rbytes == 4 ? run_chain_fused_axes<float>(ctx, segs, nseg, st, cidx)
+                            : run_chain_fused_axes<double>(ctx, segs, nseg, st, cidx);
   const long long M = ctx->M;
   float *tmp[2] = {static_cast<float *>(ctx->tmp[2 * cidx]),
                    static_cast<float *>(ctx->tmp[2 * cidx + 1])};
@@ -674,8 +676,7 @@ int autotune(scft_ctx *ctx) {
   for (size_t i = 1; i < ctx->passes.size(); ++i)
     has_fast_col |= ctx->rbytes == 4 && ctx->passes[i].use_fast != 0;
   const bool can_xy = ctx->fuse_xy;
-  const bool can_fs = (ctx->p.flags & SCFT_FLAG_NO_FUSED_STEPS) == 0 && ctx->rbytes == 4 &&
-                      ctx->passes.size() == 3;
+  const bool can_fs = (ctx->p.flags & SCFT_FLAG_NO_FUSED_STEPS) == 0 && ctx->passes.size() == 3;
   int rc;
   if ((rc = boltzmann(ctx, SCFT_FIELD_WA, ctx->st))) return rc;
   if ((rc = boltzmann(ctx, SCFT_FIELD_WB, ctx->st))) return rc;

@@ -512,34 +512,37 @@ __global__ void __launch_bounds__(256 * G, G == 1 ? 2 : 1)
 // and starts step s+1 with the factor again and the filter (stored to out).
 // Geometry, tables and the cp.async factor tile as in the column branch of
 // k_fast_line.
-template <int N, int P>
-__global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<float> ps) {
+template <typename T, int N, int P>
+__global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<T> ps) {
+  using C = typename cplx<T>::type;
   constexpr int R1 = N / P;
   constexpr int NT = P * 32;
+  constexpr int EPC = 16 / (int)sizeof(T);   // reals per 16-byte copy
+  constexpr int CPR = 64 / EPC;              // copies per tile row of 64 reals
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  float2 *ex = reinterpret_cast<float2 *>(smem_raw);
+  C *ex = reinterpret_cast<C *>(smem_raw);
   const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
   const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
   const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
-  const float *__restrict__ in = ps.in[set];
-  float *__restrict__ out = ps.out[set];
-  float *__restrict__ qo = ps.qout[set];
-  const float *__restrict__ w = ps.post[set];
-  float2 *s_tw = reinterpret_cast<float2 *>(smem_raw + fast_core_smem<float, N, false>());
-  float *s_g = reinterpret_cast<float *>(s_tw + N);
+  const T *__restrict__ in = ps.in[set];
+  T *__restrict__ out = ps.out[set];
+  T *__restrict__ qo = ps.qout[set];
+  const T *__restrict__ w = ps.post[set];
+  C *s_tw = reinterpret_cast<C *>(smem_raw + fast_core_smem<T, N, false>());
+  T *s_g = reinterpret_cast<T *>(s_tw + N);
   for (int i = threadIdx.x; i < N; i += NT) {
-    s_tw[i] = __ldg(reinterpret_cast<const float2 *>(ap.twiddle) + i);
-    s_g[i] = __ldg(reinterpret_cast<const float *>(ap.gain) + i);
+    s_tw[i] = __ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
+    s_g[i] = __ldg(reinterpret_cast<const T *>(ap.gain) + i);
   }
-  float *s_wt = reinterpret_cast<float *>(smem_raw + fast_wtile_off<float, N, false>());
+  T *s_wt = reinterpret_cast<T *>(smem_raw + fast_wtile_off<T, N, false>());
   const long long tile = (long long)blockIdx.y * ap.s_outer + (long long)blockIdx.x * 64;
   {
-    const float *wt = w + b * ps.w_bs + tile;
-    for (int c = threadIdx.x; c < N * 16; c += NT) {
-      const int row = c >> 4, part = c & 15;
+    const T *wt = w + b * ps.w_bs + tile;
+    for (int c = threadIdx.x; c < N * CPR; c += NT) {
+      const int row = c / CPR, part = c % CPR;
       asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                       smem_addr(s_wt + row * 64 + part * 4)),
-                   "l"(wt + (long long)row * ap.s_n + part * 4)
+                       smem_addr(s_wt + row * 64 + part * EPC)),
+                   "l"(wt + (long long)row * ap.s_n + part * EPC)
                    : "memory");
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
@@ -547,12 +550,12 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<float> ps) {
   pdl_wait();   // the input is the previous pass's output
   pdl_release();
   const long long base = tile + 2 * lane;
-  float2 v[R1];
+  C v[R1];
   {
-    const float *src = in + b * ps.in_bs[set] + base;
+    const T *src = in + b * ps.in_bs[set] + base;
     reg::static_for<0, R1>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
-      v[j] = __ldg(reinterpret_cast<const float2 *>(src + (long long)(p + P * j) * ap.s_n));
+      v[j] = __ldg(reinterpret_cast<const C *>(src + (long long)(p + P * j) * ap.s_n));
     });
   }
   __syncthreads();   // the shared tables are complete
@@ -560,22 +563,22 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<float> ps) {
   asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();   // every thread's tile copies are visible
   {
-    float *dq = qo + b * ps.qout_bs[set] + base;
+    T *dq = qo + b * ps.qout_bs[set] + base;
     reg::static_for<0, R1>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
-      const float2 wv = reinterpret_cast<const float2 *>(s_wt)[(p + P * j) * 32 + lane];
-      float2 r = v[j];
+      const C wv = reinterpret_cast<const C *>(s_wt)[(p + P * j) * 32 + lane];
+      C r = v[j];
       r.x *= wv.x;
       r.y *= wv.y;
-      *reinterpret_cast<float2 *>(dq + (long long)(p + P * j) * ap.s_n) = r;
-      v[j] = make_float2(r.x * wv.x, r.y * wv.y);
+      *reinterpret_cast<C *>(dq + (long long)(p + P * j) * ap.s_n) = r;
+      v[j] = mkc<C, T>(r.x * wv.x, r.y * wv.y);
     });
   }
   four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
-  float *dst = out + b * ps.out_bs[set] + base;
+  T *dst = out + b * ps.out_bs[set] + base;
   reg::static_for<0, R1>([&](auto j_) {
     constexpr int j = decltype(j_)::value;
-    *reinterpret_cast<float2 *>(dst + (long long)(p + P * j) * ap.s_n) = v[j];
+    *reinterpret_cast<C *>(dst + (long long)(p + P * j) * ap.s_n) = v[j];
   });
 }
 
@@ -583,48 +586,55 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<float> ps) {
 // k_fast_line: 64 rows per CTA staged through shared memory, pitch N+1).
 // The factor's tile (64 rows x N, contiguous in memory) is copied with
 // cp.async before the dependency wait.
-template <int N> constexpr size_t xx_wtile_off() { return fast_wtile_off<float, N, true>(); }
-template <int N> constexpr size_t xx_smem() { return xx_wtile_off<N>() + (size_t)64 * N * 4; }
+template <typename T, int N> constexpr size_t xx_wtile_off() {
+  return fast_wtile_off<T, N, true>();
+}
+template <typename T, int N> constexpr size_t xx_smem() {
+  return xx_wtile_off<T, N>() + (size_t)64 * N * sizeof(T);
+}
 
-template <int N, int P>
-__global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<float> ps) {
+template <typename T, int N, int P>
+__global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<T> ps) {
+  using C = typename cplx<T>::type;
   constexpr int R1 = N / P;
   constexpr int NT = P * 32;
   constexpr int PITCH = N + 1;
+  constexpr int EPC = 16 / (int)sizeof(T);
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  float2 *ex = reinterpret_cast<float2 *>(smem_raw);   // aliases the staging tile
-  float *stg = reinterpret_cast<float *>(smem_raw);
+  C *ex = reinterpret_cast<C *>(smem_raw);   // aliases the staging tile
+  T *stg = reinterpret_cast<T *>(smem_raw);
   const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
   const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
   const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
-  float2 *s_tw = reinterpret_cast<float2 *>(smem_raw + fast_core_smem<float, N, true>());
-  float *s_g = reinterpret_cast<float *>(s_tw + N);
+  C *s_tw = reinterpret_cast<C *>(smem_raw + fast_core_smem<T, N, true>());
+  T *s_g = reinterpret_cast<T *>(s_tw + N);
   for (int i = threadIdx.x; i < N; i += NT) {
-    s_tw[i] = __ldg(reinterpret_cast<const float2 *>(ap.twiddle) + i);
-    s_g[i] = __ldg(reinterpret_cast<const float *>(ap.gain) + i);
+    s_tw[i] = __ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
+    s_g[i] = __ldg(reinterpret_cast<const T *>(ap.gain) + i);
   }
   const long long base = (long long)blockIdx.x * 64 * N;   // 64 consecutive rows
-  float *s_wt = reinterpret_cast<float *>(smem_raw + xx_wtile_off<N>());
+  T *s_wt = reinterpret_cast<T *>(smem_raw + xx_wtile_off<T, N>());
   {
-    const float *wt = ps.post[set] + b * ps.w_bs + base;
-    for (int c = threadIdx.x; c < 16 * N; c += NT)
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(s_wt + 4 * c)),
-                   "l"(wt + 4 * c)
+    const T *wt = ps.post[set] + b * ps.w_bs + base;
+    for (int c = threadIdx.x; c < 64 * N / EPC; c += NT)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                       smem_addr(s_wt + EPC * c)),
+                   "l"(wt + EPC * c)
                    : "memory");
     asm volatile("cp.async.commit_group;" ::: "memory");
   }
   pdl_wait();   // the rows are the previous pass's output
   pdl_release();
-  const float *src = ps.in[set] + b * ps.in_bs[set] + base;
+  const T *src = ps.in[set] + b * ps.in_bs[set] + base;
 #pragma unroll
   for (int i = threadIdx.x; i < 64 * N; i += NT) stg[(i / N) * PITCH + (i % N)] = __ldg(src + i);
   __syncthreads();
-  float2 v[R1];
+  C v[R1];
   auto rows_to_regs = [&]() {
     reg::static_for<0, R1>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
       const int n = p + P * j;
-      v[j] = make_float2(stg[lane * PITCH + n], stg[(lane + 32) * PITCH + n]);
+      v[j] = mkc<C, T>(stg[lane * PITCH + n], stg[(lane + 32) * PITCH + n]);
     });
     __syncthreads();   // the staging tile is free for the exchange
   };
@@ -643,12 +653,12 @@ __global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<float> ps) {
   asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();   // every thread's tile copies are visible
   {
-    float *dq = ps.qout[set] + b * ps.qout_bs[set] + base;
+    T *dq = ps.qout[set] + b * ps.qout_bs[set] + base;
 #pragma unroll 4
     for (int i = threadIdx.x; i < 64 * N; i += NT) {
       const int o = (i / N) * PITCH + (i % N);
-      const float w = s_wt[i];
-      const float x = stg[o] * w;
+      const T w = s_wt[i];
+      const T x = stg[o] * w;
       dq[i] = x;
       stg[o] = x * w;
     }
@@ -657,7 +667,7 @@ __global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<float> ps) {
   rows_to_regs();
   four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
   regs_to_rows();
-  float *dst = ps.out[set] + b * ps.out_bs[set] + base;
+  T *dst = ps.out[set] + b * ps.out_bs[set] + base;
 #pragma unroll 4
   for (int i = threadIdx.x; i < 64 * N; i += NT) dst[i] = stg[(i / N) * PITCH + (i % N)];
 }
@@ -866,26 +876,27 @@ cudaError_t launch_xyxy_t(const AxisPlan &apx, const AxisPlan &apy, const PassSe
   return launch_pdl(k_xyxy<NX, NY, G>, grid, dim3(256 * G), xyxy_smem<NX, NY, G>(), st, apx,
                     apy, ps);
 }
-template <int N, int P> cudaError_t prep_xx() {
-  return cudaFuncSetAttribute(k_xx<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)xx_smem<N>());
+template <typename T, int N, int P> cudaError_t prep_xx() {
+  return cudaFuncSetAttribute(k_xx<T, N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)xx_smem<T, N>());
 }
-template <int N, int P>
-cudaError_t launch_xx_t(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
+template <typename T, int N, int P>
+cudaError_t launch_xx_t(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
   dim3 grid(ap.n_real / 64, 1, ps.nset * ps.batch);
-  return launch_pdl(k_xx<N, P>, grid, dim3(P * 32), xx_smem<N>(), st, ap, ps);
+  return launch_pdl(k_xx<T, N, P>, grid, dim3(P * 32), xx_smem<T, N>(), st, ap, ps);
 }
-template <int N, int P> cudaError_t prep_zz() {
-  return cudaFuncSetAttribute(k_zz<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)fast_smem<float, N, P, false>());
+template <typename T, int N, int P> cudaError_t prep_zz() {
+  return cudaFuncSetAttribute(k_zz<T, N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)fast_smem<T, N, P, false>());
 }
-template <int N, int P>
-cudaError_t launch_zz_t(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st) {
+template <typename T, int N, int P>
+cudaError_t launch_zz_t(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
   dim3 grid(ap.n_real / 64, ap.n_outer, ps.nset * ps.batch);
-  return launch_pdl(k_zz<N, P>, grid, dim3(P * 32), fast_smem<float, N, P, false>(), st, ap, ps);
+  return launch_pdl(k_zz<T, N, P>, grid, dim3(P * 32), fast_smem<T, N, P, false>(), st, ap,
+                    ps);
 }
-// 16-byte cp.async tiles and float2 lines: refuse misaligned buffers
-bool fused_aligned(const PassSet<float> &ps) {
+// 16-byte cp.async tiles and two-real lines: refuse misaligned buffers
+template <typename T> bool fused_aligned(const PassSet<T> &ps) {
   for (int k = 0; k < ps.nset; ++k)
     if ((reinterpret_cast<uintptr_t>(ps.post[k]) | reinterpret_cast<uintptr_t>(ps.in[k]) |
          reinterpret_cast<uintptr_t>(ps.out[k]) | reinterpret_cast<uintptr_t>(ps.qout[k])) & 15 ||
@@ -899,10 +910,20 @@ cudaError_t launch_xx(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t
   if (ps.nset < 1 || ps.nset > kMaxSet || !ap.n_fast) return cudaErrorInvalidValue;
   if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
   switch (ap.n) {
-    case 32: return launch_xx_t<32, 4>(ap, ps, st);
-    case 64: return launch_xx_t<64, 8>(ap, ps, st);
-    case 128: return launch_xx_t<128, 8>(ap, ps, st);
-    case 256: return launch_xx_t<256, 16>(ap, ps, st);
+    case 32: return launch_xx_t<float, 32, 4>(ap, ps, st);
+    case 64: return launch_xx_t<float, 64, 8>(ap, ps, st);
+    case 128: return launch_xx_t<float, 128, 8>(ap, ps, st);
+    case 256: return launch_xx_t<float, 256, 16>(ap, ps, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+cudaError_t launch_xx(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st) {
+  if (ps.nset < 1 || ps.nset > kMaxSet || !ap.n_fast) return cudaErrorInvalidValue;
+  if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
+  switch (ap.n) {
+    case 32: return launch_xx_t<double, 32, 4>(ap, ps, st);
+    case 64: return launch_xx_t<double, 64, 8>(ap, ps, st);
+    case 128: return launch_xx_t<double, 128, 8>(ap, ps, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -916,10 +937,20 @@ cudaError_t launch_zz(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t
   if (ps.nset < 1 || ps.nset > kMaxSet || ap.n_fast) return cudaErrorInvalidValue;
   if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
   switch (ap.n) {
-    case 32: return launch_zz_t<32, 4>(ap, ps, st);
-    case 64: return launch_zz_t<64, 8>(ap, ps, st);
-    case 128: return launch_zz_t<128, 8>(ap, ps, st);
-    case 256: return launch_zz_t<256, 16>(ap, ps, st);
+    case 32: return launch_zz_t<float, 32, 4>(ap, ps, st);
+    case 64: return launch_zz_t<float, 64, 8>(ap, ps, st);
+    case 128: return launch_zz_t<float, 128, 8>(ap, ps, st);
+    case 256: return launch_zz_t<float, 256, 16>(ap, ps, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+cudaError_t launch_zz(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st) {
+  if (ps.nset < 1 || ps.nset > kMaxSet || ap.n_fast) return cudaErrorInvalidValue;
+  if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
+  switch (ap.n) {
+    case 32: return launch_zz_t<double, 32, 4>(ap, ps, st);
+    case 64: return launch_zz_t<double, 64, 8>(ap, ps, st);
+    case 128: return launch_zz_t<double, 128, 8>(ap, ps, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -978,14 +1009,17 @@ cudaError_t fast_line_prepare() {
   if ((e = prep_xyxy<64, 64>()) != cudaSuccess) return e;
   if ((e = prep_xyxy<128, 64>()) != cudaSuccess) return e;
   if ((e = prep_xyxy<64, 128>()) != cudaSuccess) return e;
-  if ((e = prep_xx<32, 4>()) != cudaSuccess) return e;
-  if ((e = prep_xx<64, 8>()) != cudaSuccess) return e;
-  if ((e = prep_xx<128, 8>()) != cudaSuccess) return e;
-  if ((e = prep_xx<256, 16>()) != cudaSuccess) return e;
-  if ((e = prep_zz<32, 4>()) != cudaSuccess) return e;
-  if ((e = prep_zz<64, 8>()) != cudaSuccess) return e;
-  if ((e = prep_zz<128, 8>()) != cudaSuccess) return e;
-  if ((e = prep_zz<256, 16>()) != cudaSuccess) return e;
+#define PREP_FUSED(T, N, P)                                          \
+  if ((e = prep_xx<T, N, P>()) != cudaSuccess) return e;            \
+  if ((e = prep_zz<T, N, P>()) != cudaSuccess) return e;
+  PREP_FUSED(float, 32, 4)
+  PREP_FUSED(float, 64, 8)
+  PREP_FUSED(float, 128, 8)
+  PREP_FUSED(float, 256, 16)
+  PREP_FUSED(double, 32, 4)
+  PREP_FUSED(double, 64, 8)
+  PREP_FUSED(double, 128, 8)
+#undef PREP_FUSED
   return e;
 }
 

@@ -65,8 +65,10 @@ cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<double> &ps, cuda
 // run as one kernel: qout = post * K_a(in), out = K_a(post * qout), with
 // K_a the z filter (launch_zz) or the x+y filters (launch_xyxy).
 cudaError_t launch_zz(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
+cudaError_t launch_zz(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st);
 // the same on x lines (rows contiguous), for grids without the x+y plane
 cudaError_t launch_xx(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
+cudaError_t launch_xx(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st);
 cudaError_t launch_xyxy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
                         cudaStream_t st);
 
