@@ -198,6 +198,36 @@ def converge_timed(ctx, tol, max_it, budget_s):
     return total, fe, False
 
 
+def translation_aligned_diff(a, b, iters=4):
+    """max|a(r) - b(r - d)| / max|a| for the rigid shift d (in voxels, per
+    axis) that best aligns b with a, found by Gauss-Newton on the spectral
+    shift b(r - d) = IFFT[B(k) exp(-i k.d)].  A converged periodic structure
+    is only defined up to such a shift (the translational zero mode), so two
+    runs that reach the same structure may differ by it at the same F.
+    Returns (relative difference, d)."""
+    shape = a.shape
+    B = np.fft.rfftn(b)
+    ks = []
+    for ax, n in enumerate(shape):
+        f = np.fft.rfftfreq(n) if ax == len(shape) - 1 else np.fft.fftfreq(n)
+        k = 2 * np.pi * f
+        if n % 2 == 0:
+            k[n // 2 if ax < len(shape) - 1 else -1] = 0.0   # no derivative at Nyquist
+        sh = [1] * len(shape)
+        sh[ax] = k.size
+        ks.append(k.reshape(sh))
+    d = np.zeros(len(shape))
+    for _ in range(iters):
+        ph = np.exp(-1j * sum(k * dj for k, dj in zip(ks, d)))
+        s = np.fft.irfftn(B * ph, s=shape)
+        G = np.stack([np.fft.irfftn(-1j * k * B * ph, s=shape).ravel() for k in ks], axis=1)
+        r = (a - s).ravel()
+        step = np.linalg.lstsq(G, -r, rcond=None)[0]
+        d = d - step
+    s = np.fft.irfftn(B * np.exp(-1j * sum(k * dj for k, dj in zip(ks, d))), s=shape)
+    return float(np.abs(a - s).max() / np.abs(a).max()), [float(x) for x in d]
+
+
 def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
     """Seconds to converge (max-norm residual < tol) on the 64^3 double-gyroid
     config (f=0.36, chiN=18, box 3.8, Ns=200, Anderson history 20): the plain
@@ -255,6 +285,9 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
                    np.abs(np.abs(np.fft.rfftn(phamx[0])) - np.abs(np.fft.rfftn(pha64[0]))).max()
                    / np.abs(np.fft.rfftn(pha64[0])).max()),
                Q_rel_diff=float(abs(Qmx[0] - Q64[0]) / abs(Q64[0])))
+    # pointwise, after removing the rigid shift between the two structures
+    al, shift = translation_aligned_diff(pha64[0], phamx[0])
+    out.update(phiA_rel_diff_shift_aligned=al, phiA_shift_voxels=shift)
     return out
 
 
@@ -452,9 +485,11 @@ def run_ours(args):
     dev = local if ws > 1 else 0
     prec = pkg.PREC_FP64 if args.precision == "fp64" else pkg.PREC_FP32
     n, ds = args.grid, 1.0 / args.ns
-    headline = (n == N and args.ns == 200)
+    headline = (n == N and args.ns == 200 and args.mixing == "simple")
+    mix = ({"mixing": pkg.MIX_ANDERSON, "anderson_history": 20, "anderson_start": 1e9}
+           if args.mixing == "anderson" else {})
     ctx = pkg.Context(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, hAB=CHIN, fA=FA, ds0=ds,
-                      precision=prec, device=dev)
+                      precision=prec, device=dev, **mix)
     wa, wb = fl.gyroid(n, n, n, L, L, L, CHIN, seed=rank)
     ctx.set_w(wa, wb)
     pt_steps = 2 * (ctx.NsA + ctx.dNsB) * n ** 3
@@ -524,8 +559,8 @@ def run_ours(args):
         march_rate = march_pts / (march_ms / 1e3)          # pt-steps/s inside marches
         achieved = march_rate * bpp / 1e9                  # GB/s, algorithmic bytes
         workload = WORKLOAD if headline else (
-            f"{n}^3 gyroid (f=0.36, chiN=18, box 3.8), Ns={args.ns}: a reduced case for "
-            f"profiling, not the headline")
+            f"{n}^3 gyroid (f=0.36, chiN=18, box 3.8), Ns={args.ns}, {args.mixing} mixing: a "
+            f"case for profiling, not the headline")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps,
@@ -586,6 +621,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--grid", type=int, default=N, help="grid edge (profiling cases only)")
     ap.add_argument("--ns", type=int, default=200, help="contour steps 1/ds (profiling only)")
+    ap.add_argument("--mixing", default="simple", choices=["simple", "anderson"],
+                    help="field update of the timed iterations (anderson: profiling only)")
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the 64-instance heterogeneous sweep leg")
     ap.add_argument("--no-converge", action="store_true",

@@ -74,6 +74,36 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// Four doubles of one grid point (w_A, w_B, phi_A, phi_B) held in registers.
+struct dquad {
+  double x, y, z, w;
+};
+
+// Grid-stride loop over [0, n) for streaming kernels, U elements per thread
+// per trip: the elements i0, i0+S, ..., i0+(U-1)S (S = the grid's thread
+// count) are loaded first, load(i), then used, use(i, value).  The U loads of
+// a trip are independent, so a thread keeps U requests in flight instead of
+// one (a kernel with one outstanding load per thread reaches only a fraction
+// of HBM bandwidth).  Consecutive threads still touch consecutive elements.
+template <int U, typename L, typename F>
+__device__ __forceinline__ void stream_loop(long long n, L &&load, F &&use) {
+  typedef decltype(load(0LL)) V;
+  const long long S = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += U * S) {
+    V v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long i = i0 + u * S;
+      if (i < n) v[u] = load(i);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long i = i0 + u * S;
+      if (i < n) use(i, v[u]);
+    }
+  }
+}
+
 // Error-free transformation a+b = s+e (Knuth TwoSum), FP32.
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   s = a + b;

@@ -66,13 +66,14 @@ __global__ void k_residual_sum(const double *__restrict__ wa, const double *__re
   __shared__ double sh[32];
   const long long b = blockIdx.y, o = b * M;
   double sa = 0.0, sb = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
-       i += (long long)gridDim.x * blockDim.x) {
+  auto load = [&](long long i) { return dquad{wa[o + i], wb[o + i], pha[o + i], phb[o + i]}; };
+  stream_loop<4>(M, load,
+                 [&](long long, dquad v) {
     double da, db;
-    phi_w_dir(wa[o + i], wb[o + i], pha[o + i], phb[o + i], hAB, wcmp, da, db);
+    phi_w_dir(v.x, v.y, v.z, v.w, hAB, wcmp, da, db);
     sa += da;
     sb += db;
-  }
+  });
   const double ra = blk_sum(sa, sh);
   const double rb = blk_sum(sb, sh);
   if (threadIdx.x == 0) {
@@ -115,11 +116,12 @@ __global__ void k_residual(double *__restrict__ wa, double *__restrict__ wb,
   const long long b = blockIdx.y, o = b * M;
   const double ma = dmean[b * 2 + 0], mb = dmean[b * 2 + 1];
   double mx = 0.0, ss = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
-       i += (long long)gridDim.x * blockDim.x) {
-    const double a = wa[o + i], c = wb[o + i];
+  auto load = [&](long long i) { return dquad{wa[o + i], wb[o + i], pha[o + i], phb[o + i]}; };
+  stream_loop<4>(M, load,
+                 [&](long long i, dquad v) {
+    const double a = v.x, c = v.y;
     double da, db;
-    phi_w_dir(a, c, pha[o + i], phb[o + i], hAB, wcmp, da, db);   // cuda_aid.cu:398-408
+    phi_w_dir(a, c, v.z, v.w, hAB, wcmp, da, db);   // cuda_aid.cu:398-408
     const double ca = da - ma, cb = db - mb;
     mx = fmax(mx, fmax(fabs(ca), fabs(cb)));
     ss += ca * ca + cb * cb;
@@ -133,7 +135,7 @@ __global__ void k_residual(double *__restrict__ wa, double *__restrict__ wb,
       wa[o + i] = a + wopt * da;   // phi_w, cuda_aid.cu:410-412
       wb[o + i] = c + wopt * db;
     }
-  }
+  });
   const double rm = blk_max(mx, sh);
   const double rs = blk_sum(ss, sh);
   if (threadIdx.x == 0) {

@@ -45,11 +45,10 @@ __device__ __forceinline__ double block_max(double v, double *sh) {
 template <typename R>
 __global__ void k_boltzmann(const double *__restrict__ w, R *__restrict__ W, long long n,
                             double ds2) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    if constexpr (sizeof(R) == 4) W[i] = expf(-(float)w[i] * (float)ds2);
-    else W[i] = exp(-w[i] * ds2);
-  }
+  stream_loop<4>(n, [&](long long i) { return w[i]; }, [&](long long i, double x) {
+    if constexpr (sizeof(R) == 4) W[i] = expf(-(float)x * (float)ds2);
+    else W[i] = exp(-x * ds2);
+  });
 }
 
 template <typename R>
@@ -65,9 +64,7 @@ __global__ void k_copy(D *__restrict__ dst, long long dbs, const R *__restrict__
                        long long sbs, long long M) {
   D *d = dst + blockIdx.y * dbs;
   const R *s = src + blockIdx.y * sbs;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
-       i += (long long)gridDim.x * blockDim.x)
-    d[i] = (D)s[i];
+  stream_loop<4>(M, [&](long long i) { return s[i]; }, [&](long long i, R x) { d[i] = (D)x; });
 }
 
 template <typename R>
@@ -76,9 +73,8 @@ __global__ void k_partial_sum(const R *__restrict__ x, long long bs, long long M
   __shared__ double sh[32];
   const R *xb = x + blockIdx.y * bs;
   double acc = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
-       i += (long long)gridDim.x * blockDim.x)
-    acc += (double)xb[i];
+  stream_loop<8>(M, [&](long long i) { return xb[i]; },
+                 [&](long long, R x) { acc += (double)x; });
   acc = block_sum(acc, sh);
   if (threadIdx.x == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = acc;
 }
@@ -98,9 +94,8 @@ __global__ void k_minus_average(double *__restrict__ data, const double *__restr
   // minus_average (cuda_aid.cu:377) divides per element; the quotient is the
   // same for every element, so it is formed once (bit-identical result).
   const double mean = sum[blockIdx.y] / (double)M;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
-       i += (long long)gridDim.x * blockDim.x)
-    d[i] = d[i] - mean;
+  stream_loop<8>(M, [&](long long i) { return d[i]; },
+                 [&](long long i, double x) { d[i] = x - mean; });
 }
 
 __global__ void k_q_ffl(const double *__restrict__ sum, long long M, double ds0, int batch,
@@ -164,10 +159,10 @@ __global__ void k_contour_phi<float>(const float *__restrict__ q, const float *_
 __global__ void k_phi_w(double *__restrict__ wa, double *__restrict__ wb,
                         const double *__restrict__ pha, const double *__restrict__ phb,
                         double hAB, double wopt, double wcmp, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
+  stream_loop<4>(n, [&](long long i) { return dquad{wa[i], wb[i], pha[i], phb[i]}; },
+                 [&](long long i, dquad v) {
     // phi_w, cuda_aid.cu:398-412
-    const double a = wa[i], b = wb[i], pa = pha[i], pb = phb[i];
+    const double a = v.x, b = v.y, pa = v.z, pb = v.w;
     const double eta = (a + b - hAB) / 2;
     const double psum = 1.0 - pa - pb;
     double da = hAB * pb + eta - a;
@@ -176,7 +171,7 @@ __global__ void k_phi_w(double *__restrict__ wa, double *__restrict__ wb,
     db -= wcmp * psum;
     wa[i] = a + wopt * da;
     wb[i] = b + wopt * db;
-  }
+  });
 }
 
 // phi_w_constrained (cuda_aid.cu:418-452): simple mixing plus a penalty
@@ -257,13 +252,14 @@ __global__ void k_fe_partials(const double *__restrict__ wa, const double *__res
   __shared__ double sh[32];
   const long long o = blockIdx.y * M;
   double fab = 0.0, fw = 0.0, inc = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
-       i += (long long)gridDim.x * blockDim.x) {
-    const double pa = pha[o + i], pb = phb[o + i];
+  auto load = [&](long long i) { return dquad{wa[o + i], wb[o + i], pha[o + i], phb[o + i]}; };
+  stream_loop<4>(M, load,
+                 [&](long long, dquad v) {
+    const double pa = v.z, pb = v.w;
     fab += hAB * pa * pb;                          // cuda_scft.cu:207
-    fw += wa[o + i] * pa + wb[o + i] * pb;         // cuda_scft.cu:208
+    fw += v.x * pa + v.y * pb;                     // cuda_scft.cu:208
     inc = fmax(inc, fabs(1.0 - pa - pb));          // cuda_scft.cu:203-206
-  }
+  });
   const int nb = gridDim.x;
   double r;
   r = block_sum(fab, sh);
@@ -309,7 +305,7 @@ inline int grid_for(long long n) {
 
 int reduce_blocks(long long M) {
   long long g = (M + kThreads * 4 - 1) / (kThreads * 4);
-  if (g > 304) g = 304;
+  if (g > 152 * 4) g = 152 * 4;
   if (g < 1) g = 1;
   return (int)g;
 }
