@@ -206,6 +206,7 @@ def translation_aligned_diff(a, b, iters=4):
     runs that reach the same structure may differ by it at the same F.
     Returns (relative difference, d)."""
     shape = a.shape
+    axes = tuple(range(a.ndim))
     B = np.fft.rfftn(b)
     ks = []
     for ax, n in enumerate(shape):
@@ -219,12 +220,13 @@ def translation_aligned_diff(a, b, iters=4):
     d = np.zeros(len(shape))
     for _ in range(iters):
         ph = np.exp(-1j * sum(k * dj for k, dj in zip(ks, d)))
-        s = np.fft.irfftn(B * ph, s=shape)
-        G = np.stack([np.fft.irfftn(-1j * k * B * ph, s=shape).ravel() for k in ks], axis=1)
+        s = np.fft.irfftn(B * ph, s=shape, axes=axes)
+        G = np.stack([np.fft.irfftn(-1j * k * B * ph, s=shape, axes=axes).ravel() for k in ks],
+                     axis=1)
         r = (a - s).ravel()
         step = np.linalg.lstsq(G, -r, rcond=None)[0]
         d = d - step
-    s = np.fft.irfftn(B * np.exp(-1j * sum(k * dj for k, dj in zip(ks, d))), s=shape)
+    s = np.fft.irfftn(B * np.exp(-1j * sum(k * dj for k, dj in zip(ks, d))), s=shape, axes=axes)
     return float(np.abs(a - s).max() / np.abs(a).max()), [float(x) for x in d]
 
 

@@ -48,6 +48,36 @@ __device__ __forceinline__ double blk_max(double v, double *sh) {
   return r;
 }
 
+// |x| as an ordered integer key: for non-negative doubles the unsigned bit
+// patterns order like the values, and a NaN (sign cleared) sorts above +inf,
+// so a maximum over keys propagates NaN where fmax would drop it (a diverged
+// field then reports a NaN residual instead of a finite one).
+__device__ __forceinline__ unsigned long long abs_key(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+}
+__device__ __forceinline__ unsigned long long key_max(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+__device__ __forceinline__ unsigned long long blk_max_key(unsigned long long v,
+                                                          unsigned long long *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = key_max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  unsigned long long r = 0;
+  if (wid == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0ULL;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r = key_max(r, __shfl_xor_sync(0xffffffffu, r, o));
+  }
+  return r;
+}
+
+// phi_w's update direction (cuda_aid.cu:398-408).  It is affine in
+// (wA, wB, phiA, phiB), so the instance mean of the direction is the
+// direction of the instance means.
 __device__ __forceinline__ void phi_w_dir(double a, double c, double pa, double pb, double hAB,
                                           double wcmp, double &da, double &db) {
   const double eta = (a + c - hAB) / 2;
@@ -58,45 +88,40 @@ __device__ __forceinline__ void phi_w_dir(double a, double c, double pa, double 
   db -= wcmp * psum;
 }
 
-// Per-instance sums of dA and dB: partial[(b*2 + f)*nblk + blk].
+// Per-instance sums of wA, wB, phiA, phiB: partial[(b*4 + f)*nblk + blk].
+// (Four additions per point: GB300's FP64 pipe, not HBM, bounds the
+// per-point direction, so its mean is formed from these sums instead.)
 __global__ void k_residual_sum(const double *__restrict__ wa, const double *__restrict__ wb,
                                const double *__restrict__ pha, const double *__restrict__ phb,
-                               double hAB, double wcmp, long long M,
-                               double *__restrict__ partial) {
+                               long long M, double *__restrict__ partial) {
   __shared__ double sh[32];
   const long long b = blockIdx.y, o = b * M;
-  double sa = 0.0, sb = 0.0;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
   auto load = [&](long long i) { return dquad{wa[o + i], wb[o + i], pha[o + i], phb[o + i]}; };
-  stream_loop<4>(M, load,
-                 [&](long long, dquad v) {
-    double da, db;
-    phi_w_dir(v.x, v.y, v.z, v.w, hAB, wcmp, da, db);
-    sa += da;
-    sb += db;
+  stream_loop<4>(M, load, [&](long long, dquad v) {
+    s0 += v.x;
+    s1 += v.y;
+    s2 += v.z;
+    s3 += v.w;
   });
-  const double ra = blk_sum(sa, sh);
-  const double rb = blk_sum(sb, sh);
-  if (threadIdx.x == 0) {
-    partial[(b * 2 + 0) * gridDim.x + blockIdx.x] = ra;
-    partial[(b * 2 + 1) * gridDim.x + blockIdx.x] = rb;
-  }
+  const double r[4] = {blk_sum(s0, sh), blk_sum(s1, sh), blk_sum(s2, sh), blk_sum(s3, sh)};
+  if (threadIdx.x == 0)
+    for (int f = 0; f < 4; ++f) partial[(b * 4 + f) * gridDim.x + blockIdx.x] = r[f];
 }
 
-// dmean[b*2 + f] = mean of dA / dB
+// dmean[b*2 + f] = mean of dA / dB = the direction of the field means
 __global__ void k_residual_mean(const double *__restrict__ partial, int nblk, long long M,
-                                double *__restrict__ dmean) {
+                                double hAB, double wcmp, double *__restrict__ dmean) {
   __shared__ double sh[32];
   const int b = blockIdx.x;
-  double sa = 0.0, sb = 0.0;
-  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
-    sa += partial[(b * 2 + 0) * nblk + i];
-    sb += partial[(b * 2 + 1) * nblk + i];
-  }
-  sa = blk_sum(sa, sh);
-  sb = blk_sum(sb, sh);
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x)
+    for (int f = 0; f < 4; ++f) s[f] += partial[(b * 4 + f) * nblk + i];
+  for (int f = 0; f < 4; ++f) s[f] = blk_sum(s[f], sh);
   if (threadIdx.x == 0) {
-    dmean[b * 2 + 0] = sa / (double)M;
-    dmean[b * 2 + 1] = sb / (double)M;
+    const double m = (double)M;
+    phi_w_dir(s[0] / m, s[1] / m, s[2] / m, s[3] / m, hAB, wcmp, dmean[b * 2 + 0],
+              dmean[b * 2 + 1]);
   }
 }
 
@@ -113,9 +138,11 @@ __global__ void k_residual(double *__restrict__ wa, double *__restrict__ wb,
                            const double *__restrict__ dmean, double *__restrict__ hw,
                            double *__restrict__ hd, double *__restrict__ partial) {
   __shared__ double sh[32];
+  __shared__ unsigned long long shk[32];
   const long long b = blockIdx.y, o = b * M;
   const double ma = dmean[b * 2 + 0], mb = dmean[b * 2 + 1];
-  double mx = 0.0, ss = 0.0;
+  unsigned long long mx = 0;
+  double ss = 0.0;
   auto load = [&](long long i) { return dquad{wa[o + i], wb[o + i], pha[o + i], phb[o + i]}; };
   stream_loop<4>(M, load,
                  [&](long long i, dquad v) {
@@ -123,7 +150,7 @@ __global__ void k_residual(double *__restrict__ wa, double *__restrict__ wb,
     double da, db;
     phi_w_dir(a, c, v.z, v.w, hAB, wcmp, da, db);   // cuda_aid.cu:398-408
     const double ca = da - ma, cb = db - mb;
-    mx = fmax(mx, fmax(fabs(ca), fabs(cb)));
+    mx = key_max(mx, key_max(abs_key(ca), abs_key(cb)));
     ss += ca * ca + cb * cb;
     if (hw) {
       hw[(2 * b) * M + i] = a;
@@ -136,10 +163,10 @@ __global__ void k_residual(double *__restrict__ wa, double *__restrict__ wb,
       wb[o + i] = c + wopt * db;
     }
   });
-  const double rm = blk_max(mx, sh);
+  const unsigned long long rm = blk_max_key(mx, shk);
   const double rs = blk_sum(ss, sh);
   if (threadIdx.x == 0) {
-    partial[(b * 2 + 0) * gridDim.x + blockIdx.x] = rm;
+    partial[(b * 2 + 0) * gridDim.x + blockIdx.x] = __longlong_as_double((long long)rm);
     partial[(b * 2 + 1) * gridDim.x + blockIdx.x] = rs;
   }
 }
@@ -148,16 +175,18 @@ __global__ void k_residual(double *__restrict__ wa, double *__restrict__ wb,
 __global__ void k_residual_finalize(const double *__restrict__ partial, int nblk, long long M,
                                     double *__restrict__ err) {
   __shared__ double sh[32];
+  __shared__ unsigned long long shk[32];
   const int b = blockIdx.x;
-  double mx = 0.0, ss = 0.0;
+  unsigned long long mx = 0;
+  double ss = 0.0;
   for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
-    mx = fmax(mx, partial[(b * 2 + 0) * nblk + i]);
+    mx = key_max(mx, abs_key(partial[(b * 2 + 0) * nblk + i]));
     ss += partial[(b * 2 + 1) * nblk + i];
   }
-  mx = blk_max(mx, sh);
+  mx = blk_max_key(mx, shk);
   ss = blk_sum(ss, sh);
   if (threadIdx.x == 0) {
-    err[b * 2 + 0] = mx;
+    err[b * 2 + 0] = __longlong_as_double((long long)mx);
     err[b * 2 + 1] = sqrt(ss / (2.0 * (double)M));
   }
 }
@@ -170,25 +199,43 @@ struct SlotList {
   int slot[kMaxSlots];
   int n;
 };
+// Grid row blockIdx.y takes the kChunk list entries from blockIdx.y*kChunk:
+// few accumulators keep the occupancy high and each thread has kChunk + 1
+// loads in flight per element; d_c is read once per chunk (an L2 hit while
+// it fits).
+constexpr int kChunk = 8;
 __global__ void k_gram_row(const double *__restrict__ dc, SlotList sl, long long M,
                            double *__restrict__ partial) {
   __shared__ double sh[32];
-  const long long b = blockIdx.y;
-  double acc[kMaxSlots];
-#pragma unroll
-  for (int k = 0; k < kMaxSlots; ++k) acc[k] = 0.0;
+  const long long b = blockIdx.z;
+  const int k0 = blockIdx.y * kChunk;
   const long long n2 = 2 * M;
+  const double *dk[kChunk];
+  double acc[kChunk];
+#pragma unroll
+  for (int kk = 0; kk < kChunk; ++kk) {
+    dk[kk] = k0 + kk < sl.n ? sl.d[k0 + kk] + b * n2 : nullptr;
+    acc[kk] = 0.0;
+  }
+  const double *x = dc + b * n2;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2;
        i += (long long)gridDim.x * blockDim.x) {
-    const double x = dc[b * n2 + i];
+    double y[kChunk];
 #pragma unroll
-    for (int k = 0; k < kMaxSlots; ++k)
-      if (k < sl.n) acc[k] += x * sl.d[k][b * n2 + i];
+    for (int kk = 0; kk < kChunk; ++kk)
+      if (dk[kk]) y[kk] = dk[kk][i];
+    const double xi = x[i];
+#pragma unroll
+    for (int kk = 0; kk < kChunk; ++kk)
+      if (dk[kk]) acc[kk] += xi * y[kk];
   }
-#pragma unroll 1
-  for (int k = 0; k < sl.n; ++k) {
-    const double r = blk_sum(acc[k], sh);
-    if (threadIdx.x == 0) partial[(b * kMaxSlots + k) * gridDim.x + blockIdx.x] = r;
+#pragma unroll
+  for (int kk = 0; kk < kChunk; ++kk) {
+    if (dk[kk]) {
+      const double r = blk_sum(acc[kk], sh);
+      if (threadIdx.x == 0)
+        partial[(b * kMaxSlots + k0 + kk) * gridDim.x + blockIdx.x] = r;
+    }
   }
 }
 
@@ -299,15 +346,18 @@ struct SlotPairs {
 __global__ void k_anderson_update(double *__restrict__ wa, double *__restrict__ wb,
                                   SlotPairs sp, const double *__restrict__ a,
                                   const double *__restrict__ lam, int m1, long long M) {
+  __shared__ double s_a[kMaxSlots];   // the weights of the listed slots
   const long long b = blockIdx.y;
   const double l = lam[b];
   const long long n2 = 2 * M;
+  for (int k = threadIdx.x; k < sp.n; k += blockDim.x) s_a[k] = a[b * m1 + sp.idx[k]];
+  __syncthreads();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2;
        i += (long long)gridDim.x * blockDim.x) {
     double s = 0.0;
 #pragma unroll 4
     for (int k = 0; k < sp.n; ++k) {
-      const double aj = a[b * m1 + sp.idx[k]];
+      const double aj = s_a[k];
       if (aj != 0.0) s += aj * (sp.w[k][b * n2 + i] + l * sp.d[k][b * n2 + i]);
     }
     if (i < M) wa[b * M + i] = s;
@@ -331,8 +381,8 @@ cudaError_t launch_residual(double *wa, double *wb, const double *pha, const dou
                             cudaStream_t st) {
   // err holds [b][2] results; err + 2*batch holds the [b][2] means of dA, dB
   double *dmean = err + 2 * batch;
-  k_residual_sum<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, wcmp, M, partial);
-  k_residual_mean<<<batch, kThreads, 0, st>>>(partial, nblk, M, dmean);
+  k_residual_sum<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, pha, phb, M, partial);
+  k_residual_mean<<<batch, kThreads, 0, st>>>(partial, nblk, M, hAB, wcmp, dmean);
   k_residual<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, wcmp, wopt, M, dmean,
                                                     hw, hd, partial);
   k_residual_finalize<<<batch, kThreads, 0, st>>>(partial, nblk, M, err);
@@ -348,7 +398,8 @@ cudaError_t launch_gram_row(const double *dc, const double *const *dj, const int
     sl.d[k] = dj[k];
     sl.slot[k] = slots[k];
   }
-  k_gram_row<<<dim3(nblk, batch), kThreads, 0, st>>>(dc, sl, M, partial);
+  k_gram_row<<<dim3(nblk, (n + kChunk - 1) / kChunk, batch), kThreads, 0, st>>>(dc, sl, M,
+                                                                              partial);
   k_gram_finalize<<<dim3(n, batch), kThreads, 0, st>>>(partial, nblk, sl, c, m1, G);
   return cudaGetLastError();
 }

@@ -92,8 +92,12 @@ __global__ void k_minus_average(double *__restrict__ data, const double *__restr
                                 long long M) {
   double *d = data + blockIdx.y * M;
   // minus_average (cuda_aid.cu:377) divides per element; the quotient is the
-  // same for every element, so it is formed once (bit-identical result).
-  const double mean = sum[blockIdx.y] / (double)M;
+  // same for every element, so it is formed once per block (bit-identical
+  // result; an FP64 division per thread costs more than the whole pass).
+  __shared__ double s_mean;
+  if (threadIdx.x == 0) s_mean = sum[blockIdx.y] / (double)M;
+  __syncthreads();
+  const double mean = s_mean;
   stream_loop<8>(M, [&](long long i) { return d[i]; },
                  [&](long long i, double x) { d[i] = x - mean; });
 }

@@ -43,3 +43,23 @@ def test_diverging_iteration_is_reported(pkg):
             ctx.converge(1e-8, 2000)
         assert e.value.status == pkg.ERR_NOT_FINITE
     assert usable(pkg)
+
+
+@pytest.mark.parametrize("mixing", ["simple", "anderson"])
+def test_nan_field_is_reported_not_converged(pkg, mixing):
+    """One NaN point spreads through the propagators to every point; the
+    residual max-norm must come out NaN (a plain fmax reduction drops NaNs
+    and would report 0, i.e. converged), so converge stops at the first
+    check with SCFT_ERR_NOT_FINITE."""
+    from scft_gb300 import fields
+    wa, wb = fields.lamellar(16, 16, 16, 4.0, 4.0, 4.0, 20.0, seed=2)
+    wa.reshape(-1)[123] = np.nan
+    kw = {"mixing": pkg.MIX_ANDERSON, "anderson_history": 5} if mixing == "anderson" else {}
+    with pkg.Context(nx=16, ny=16, nz=16, **kw) as ctx:
+        ctx.set_w(wa, wb)
+        with pytest.raises(pkg.ScftError) as e:
+            ctx.converge(1e-6, 5)
+        assert e.value.status == pkg.ERR_NOT_FINITE
+        mx, rms = ctx.residual()
+        assert np.isnan(mx[0]) and np.isnan(rms[0])
+    assert usable(pkg)
