@@ -255,6 +255,9 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
         t64 = time.perf_counter() - t0
         r64 = float(c64.residual()[0][0])
         pha64, Q64 = c64.pha, c64.Q()
+        # untimed: on to 1e-7, for the correctness comparison at a tighter tolerance
+        _, fe64t, ok64t = converge_timed(c64, 1e-7, 1000, 40.0)
+        tight64 = (c64.pha, c64.phb, c64.Q(), fe64t, ok64t)
     with pkg.Context(precision=pkg.PREC_FP32, **kw) as c32, \
             pkg.Context(precision=pkg.PREC_FP64, **kw) as pol:
         c32.set_w(wa, wb)
@@ -271,6 +274,8 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
         tmx = time.perf_counter() - t0
         rmx = float(pol.residual()[0][0])
         phamx, Qmx = pol.pha, pol.Q()
+        _, fept, okpt = converge_timed(pol, 1e-7, 1000, 40.0)
+        tightmx = (pol.pha, pol.phb, pol.Q(), fept, okpt)
     out.update(fp64={"seconds": t64, "iterations": it64, "F": fe64[0, 0], "residual": r64,
                      "converged": ok64},
                fp32_fp64_polish={"seconds": tmx, "iterations_fp32": it32,
@@ -290,6 +295,16 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
     # pointwise, after removing the rigid shift between the two structures
     al, shift = translation_aligned_diff(pha64[0], phamx[0])
     out.update(phiA_rel_diff_shift_aligned=al, phiA_shift_voxels=shift)
+    # both runs continued (untimed) to a max-norm residual of 1e-7
+    if tight64[4] and tightmx[4]:
+        ala, _ = translation_aligned_diff(tight64[0][0], tightmx[0][0])
+        alb, _ = translation_aligned_diff(tight64[1][0], tightmx[1][0])
+        out["at_tol_1e-7"] = {
+            "phiA_rel_diff_shift_aligned": ala, "phiB_rel_diff_shift_aligned": alb,
+            "Q_rel_diff": float(abs(tightmx[2][0] - tight64[2][0]) / abs(tight64[2][0])),
+            "F_abs_diff": float(abs(tightmx[3][0, 0] - tight64[3][0, 0]))}
+    else:
+        out["at_tol_1e-7"] = {"converged": [bool(tight64[4]), bool(tightmx[4])]}
     return out
 
 

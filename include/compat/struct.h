@@ -89,6 +89,11 @@ typedef struct {
   /* 1: qa_cu/qb_cu/qca_cu/qcb_cu are FP64 mirrors in the reference's
    * g[b][r][s] layout (set by -DSCFT_COMPAT_FP64_LAYOUT in the driver) */
   int reference_layout = SCFT_COMPAT_REFERENCE_LAYOUT;
+  /* ab.txt as parsed by scft_read_ab_txt, with its optional keys (mixing,
+   * Anderson history/lambda/start, wopt, wcmp, precision, Ns) */
+  scft_params opts = {};
+  /* -metrics=<path>: JSON-lines progress reports (scft_set_metrics_file) */
+  char metrics[256] = {};
 } CUFFT_INFO;
 
 #endif

@@ -277,8 +277,35 @@ const char *scft_noalloc_last_error(void);
 
 /* ---- file formats (drop-in I/O) ---- */
 
-/* Parse an ab.txt file (init.cpp:81-94) into *p (other fields default). */
+/* Parse an ab.txt file (init.cpp:81-94) into *p (other fields default).
+ * After the reference's seven lines, optional `key=value` lines (one per
+ * line, no reference counterpart) set: mixing=simple|anderson, history=<m>,
+ * lambda=<Anderson step>, start=<Anderson switch residual>, wopt=, wcmp=,
+ * precision=fp32|fp64, Ns=<contour steps> (ds0 = 1/Ns).  An unknown key or a
+ * bad value is SCFT_ERR_IO. */
 int scft_read_ab_txt(const char *path, scft_params *p, int *intag);
+
+/* ---- checkpoint / metrics (no reference counterpart) ---- */
+
+/* Binary FP64 checkpoint for an exact resume (the reference's pha_<i>.dat
+ * keeps 6 significant digits).  Holds the parameters and wa, wb, phiA, phiB
+ * of every instance; with with_history != 0 and Anderson mixing also the
+ * history ring, its Gram matrix and the iteration count, so that a run
+ * resumed with the same schedule repeats the uninterrupted run bit for bit. */
+int scft_save_checkpoint(scft_ctx *ctx, const char *path, int with_history);
+/* Restore a checkpoint into a context of the same grid and batch
+ * (SCFT_ERR_INVALID_ARG otherwise).  The history is restored only when the
+ * precision, mixing, history length, box, xN, fA and ds0 also match;
+ * otherwise it restarts. */
+int scft_load_checkpoint(scft_ctx *ctx, const char *path);
+
+/* JSON-lines metrics: with a path set, every progress report of scft_free
+ * also appends one line per instance,
+ *   {"iteration":..,"instance":..,"F":..,"F_AB":..,"F_W":..,"F_S":..,
+ *    "inCompMax":..,"residual_max":..,"residual_rms":..,"elapsed_s":..}
+ * (residual: the mean-free max-norm and RMS of phi_w's update direction).
+ * NULL or "" turns it off.  The file is opened for appending on each report. */
+int scft_set_metrics_file(scft_ctx *ctx, const char *path);
 
 /* Read phi_<idx>.dat (init_cuda.cu:435-456) for instance `inst` of the
  * context: pha/phb/wa/wb columns after two header lines.  The fields are

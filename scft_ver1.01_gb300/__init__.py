@@ -40,6 +40,7 @@ EXPORTS = [
     "scft_copy_fields", "scft_group_create", "scft_group_destroy", "scft_group_last_error",
     "scft_group_iterate", "scft_group_time_iterations", "scft_group_launch_count",
     "scft_get_schedule", "scft_write_vtk", "scft_convert_pha_to_vtk", "scft_set_target",
+    "scft_save_checkpoint", "scft_load_checkpoint", "scft_set_metrics_file",
     "scft_phi_w_constrained", "scft_set_box", "scft_stress", "scft_adjoint",
     "scft_adjoint_checkpoints", "scft_relax_cell", "scft_get_box", "scft_field_device_ptr",
     "scft_get_stream", "scft_copy_q_reference_layout", "scft_selftest_bounded_wait", "scft_spline", "scft_spline_eval",
@@ -126,6 +127,9 @@ def load_library(path: str | None = None):
         "scft_get_schedule": (C.c_int, [vp, C.POINTER(C.c_int), dp]),
         "scft_write_vtk": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_char_p]),
         "scft_convert_pha_to_vtk": (C.c_int, [C.c_char_p, C.c_char_p]),
+        "scft_save_checkpoint": (C.c_int, [vp, C.c_char_p, C.c_int]),
+        "scft_load_checkpoint": (C.c_int, [vp, C.c_char_p]),
+        "scft_set_metrics_file": (C.c_int, [vp, C.c_char_p]),
         "scft_set_target": (C.c_int, [vp, dp]),
         "scft_phi_w_constrained": (C.c_int, [vp, C.c_int, C.c_double]),
         "scft_set_box": (C.c_int, [vp, C.c_double, C.c_double, C.c_double]),
@@ -411,6 +415,19 @@ class Context:
     def write_vtk(self, path: str, inst: int = 0, source: str = "pha.dat"):
         """phiA - phiB of one instance as the reference converter's VTK file."""
         self._ck(self.lib.scft_write_vtk(self.h, path.encode(), inst, source.encode()))
+
+    def save_checkpoint(self, path: str, with_history: bool = True):
+        """Binary FP64 checkpoint (fields, and the Anderson history when kept)
+        for an exact resume."""
+        self._ck(self.lib.scft_save_checkpoint(self.h, str(path).encode(), int(with_history)))
+
+    def load_checkpoint(self, path: str):
+        """Restore a checkpoint written by save_checkpoint (same grid and batch)."""
+        self._ck(self.lib.scft_load_checkpoint(self.h, str(path).encode()))
+
+    def set_metrics_file(self, path):
+        """JSON-lines progress reports of free() to `path` (None: off)."""
+        self._ck(self.lib.scft_set_metrics_file(self.h, str(path).encode() if path else None))
 
     def set_target(self, pha_target: np.ndarray):
         """Target phiA of the constrained updates ([batch, Nz, Ny, Nx] or [Nz, Ny, Nx])."""

@@ -2,6 +2,7 @@
 // propagator march, getConc, mixing, free energy and the SCF loop.  Host
 // code only; kernels live in k_line.cu / k_fields.cu.
 #include <math.h>
+#include <chrono>
 #include <cmath>
 #include <stdio.h>
 #include <string.h>
@@ -1156,9 +1157,35 @@ int scft_iterate(scft_ctx *ctx, int n_iter, double *out5) {
   return SCFT_OK;
 }
 
+int scft_set_metrics_file(scft_ctx *ctx, const char *path) {
+  if (!ctx) return SCFT_ERR_INVALID_ARG;
+  ctx->metrics_path = path ? path : "";
+  return SCFT_OK;
+}
+
+namespace {
+// One JSON line per instance for a progress report (scft_set_metrics_file).
+int write_metrics(scft_ctx *ctx, int iter, const double *fe, double elapsed_s) {
+  std::vector<double> mx(ctx->batch), rms(ctx->batch);
+  int rc = scft_get_residual(ctx, mx.data(), rms.data());
+  if (rc) return rc;
+  FILE *fp = fopen(ctx->metrics_path.c_str(), "a");
+  if (!fp) return scft_fail(ctx, SCFT_ERR_IO, "cannot append to " + ctx->metrics_path);
+  for (int i = 0; i < ctx->batch; ++i)
+    fprintf(fp,
+            "{\"iteration\":%d,\"instance\":%d,\"F\":%.17g,\"F_AB\":%.17g,\"F_W\":%.17g,"
+            "\"F_S\":%.17g,\"inCompMax\":%.17g,\"residual_max\":%.17g,"
+            "\"residual_rms\":%.17g,\"elapsed_s\":%.6f}\n",
+            iter, i, fe[5 * i + 0], fe[5 * i + 1], fe[5 * i + 2], fe[5 * i + 3], fe[5 * i + 4],
+            mx[i], rms[i], elapsed_s);
+  return fclose(fp) == 0 ? SCFT_OK : scft_fail(ctx, SCFT_ERR_IO, "write " + ctx->metrics_path);
+}
+}  // namespace
+
 int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir) {
   if (!ctx || max_it < 0 || aver_it < 1) return SCFT_ERR_INVALID_ARG;
   std::vector<double> fe(5 * ctx->batch);
+  const auto t0 = std::chrono::steady_clock::now();
   int iter = 0;
   do {                                   // cuda_scft.cu:167-253
     iter = iter + 1;
@@ -1171,6 +1198,11 @@ int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir) {
         printf("GPU %d batch %d: %5d : %.8e, %.8e, %.8e,%.8e, %.8e\n", 0, i, iter, fe[5 * i + 0],
                fe[5 * i + 1], fe[5 * i + 2], fe[5 * i + 3], fe[5 * i + 4]);
       fflush(stdout);
+      if (!ctx->metrics_path.empty()) {
+        const double el =
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if ((rc = write_metrics(ctx, iter, fe.data(), el))) return rc;
+      }
       if (outdir && iter % (aver_it * 10) == 0) {
         for (int i = 0; i < ctx->batch; ++i) {
           std::string path = std::string(outdir) + "/pha_" + std::to_string(i + 1) + ".dat";

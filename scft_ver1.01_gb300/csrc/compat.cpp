@@ -97,6 +97,8 @@ int init_scft(CUFFT_INFO *cufft_info, GPU_INFO *gpu_info, int argc, char **argv)
   }
   const char *prec = flag_value(argc, argv, "precision");
   cufft_info->precision = (prec && !strcasecmp(prec, "fp32")) ? SCFT_PREC_FP32 : SCFT_PREC_FP64;
+  const char *metrics = flag_value(argc, argv, "metrics");
+  snprintf(cufft_info->metrics, sizeof cufft_info->metrics, "%s", metrics ? metrics : "");
   if (type) {
     if (!strcasecmp(type, "GPU")) gpu_info->kernal_type = 1;
     else if (!strcasecmp(type, "CPU")) gpu_info->kernal_type = 2;
@@ -114,6 +116,8 @@ int init_scft(CUFFT_INFO *cufft_info, GPU_INFO *gpu_info, int argc, char **argv)
       exit(1);
     }
     cufft_info->intag = intag;
+    cufft_info->opts = p;
+    if (!prec) cufft_info->precision = p.precision;   // the -precision flag wins over ab.txt
     cufft_info->hAB = p.hAB;
     cufft_info->fA = p.fA;
     cufft_info->lx = p.lx; cufft_info->ly = p.ly; cufft_info->lz = p.lz;
@@ -162,8 +166,8 @@ void initialize_cufft(GPU_INFO *gpu_info, CUFFT_INFO *c) {
   c->dy = c->ly / (double)Ny;
   c->dz = c->lz / (double)Nz;
 
-  scft_params p;
-  scft_params_default(&p);
+  scft_params p = c->opts;   // ab.txt's optional keys (defaults when absent)
+  if (p.ds0 == 0.0) scft_params_default(&p);   // not parsed by init_scft: the defaults
   p.nx = Nx; p.ny = Ny; p.nz = Nz;
   p.lx = c->lx; p.ly = c->ly; p.lz = c->lz;
   p.hAB = c->hAB; p.fA = c->fA; p.ds0 = c->ds0;
@@ -179,6 +183,7 @@ void initialize_cufft(GPU_INFO *gpu_info, CUFFT_INFO *c) {
   printf("Wonderful We have successfully initialized GPU setting.\n");
   printf("Wonderful We have successfully initialized cufft setting.\n");
   scft_ctx *ctx = c->gb300;
+  if (c->metrics[0]) scft_set_metrics_file(ctx, c->metrics);
   const long M = c->NxNyNz;
   // host arrays and wave-number tables (init_cuda.cu:380-428)
   c->wa = (double *)calloc(M * c->Num_SCFT, sizeof(double));

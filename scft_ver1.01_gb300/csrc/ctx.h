@@ -30,6 +30,7 @@ struct scft_ctx {
   cudaGraphExec_t march_exec = nullptr;
   long long march_nodes = 0;    // kernel launches inside the graph
   std::string err;
+  std::string metrics_path;     // JSON-lines progress reports of scft_free ("" = off)
   long long launches = 0;
 
   // FP64 fields [batch][M]

@@ -2,6 +2,7 @@
 // phi_<i>.dat input (init_cuda.cu:435-456), pha_<i>.dat output
 // (cuda_scft.cu:233-243) and the VTK converter's output (vtk.c).  Unlike the reference, a missing or malformed file
 // is reported as SCFT_ERR_IO instead of crashing on fscanf(NULL).
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -26,8 +27,59 @@ int scft_read_ab_txt(const char *path, scft_params *p, int *intag) {
   n += fscanf(fp, "Nx=%d, Ny=%d, Nz=%d\n", &p->nx, &p->ny, &p->nz);
   n += fscanf(fp, "ds0=%lf\n", &p->ds0);
   n += fscanf(fp, "batch=%d\n", &p->batch);
+  if (n != 11) {
+    fclose(fp);
+    return scft_fail(nullptr, SCFT_ERR_IO, std::string("malformed ab.txt: ") + path);
+  }
+  // optional key=value lines after the reference's seven
+  char line[256];
+  while (fgets(line, sizeof line, fp)) {
+    std::string l(line);
+    while (!l.empty() && (l.back() == '\n' || l.back() == '\r' || l.back() == ' ')) l.pop_back();
+    if (l.empty()) continue;
+    const size_t eq = l.find('=');
+    std::string err;
+    if (eq == std::string::npos) {
+      err = "not a key=value line";
+    } else {
+      const std::string key = l.substr(0, eq), val = l.substr(eq + 1);
+      char *end = nullptr;
+      const double x = strtod(val.c_str(), &end);
+      const bool num = end && end != val.c_str() && *end == '\0';
+      if (key == "mixing") {
+        if (val == "simple") p->mixing = SCFT_MIX_SIMPLE;
+        else if (val == "anderson") p->mixing = SCFT_MIX_ANDERSON;
+        else err = "mixing must be simple or anderson";
+      } else if (key == "precision") {
+        if (val == "fp32") p->precision = SCFT_PREC_FP32;
+        else if (val == "fp64") p->precision = SCFT_PREC_FP64;
+        else err = "precision must be fp32 or fp64";
+      } else if (!num) {
+        err = "not a number";
+      } else if (key == "history") {
+        p->anderson_history = (int)x;
+      } else if (key == "lambda") {
+        p->anderson_lambda = x;
+      } else if (key == "start") {
+        p->anderson_start = x;
+      } else if (key == "wopt") {
+        p->wopt = x;
+      } else if (key == "wcmp") {
+        p->wcmp = x;
+      } else if (key == "Ns") {
+        if (x >= 1) p->ds0 = 1.0 / x;
+        else err = "Ns must be >= 1";
+      } else {
+        err = "unknown key";
+      }
+    }
+    if (!err.empty()) {
+      fclose(fp);
+      return scft_fail(nullptr, SCFT_ERR_IO,
+                       std::string(path) + ": " + err + " in line '" + l + "'");
+    }
+  }
   fclose(fp);
-  if (n != 11) return scft_fail(nullptr, SCFT_ERR_IO, std::string("malformed ab.txt: ") + path);
   if (intag) *intag = tag;
   return SCFT_OK;
 }
@@ -189,6 +241,141 @@ int scft_write_vtk(scft_ctx *ctx, const char *path, int inst, const char *source
                      through_g(p.lz / (double)p.nz), a) != SCFT_OK)
     return scft_fail(ctx, SCFT_ERR_IO, std::string("cannot write ") + path);
   return SCFT_OK;
+}
+
+}  // extern "C"
+
+// ---- binary FP64 checkpoint (no reference counterpart) -------------------
+//
+// Layout (native byte order; both machines this builds for are little-endian):
+//   char[8] "SCFTCKP1", int32 version (1),
+//   int32 nx, ny, nz, batch, precision, mixing, anderson_history, has_history,
+//   double lx, ly, lz, hAB, fA, ds0, int64 and_count,
+//   double wa, wb, phiA, phiB   [batch][M] each,
+//   double residual             [batch][4]   (norms and means of the last update)
+//   with has_history: int32 m1, then m1 rings of w and m1 rings of d
+//   ([batch][2][M] each) and the Gram matrix [batch][m1][m1].
+namespace {
+
+struct CkptHeader {
+  char magic[8];
+  int32_t version, nx, ny, nz, batch, precision, mixing, history, has_history;
+  double lx, ly, lz, hAB, fA, ds0;
+  int64_t and_count;
+};
+
+// device <-> file through a bounded host buffer
+int dev_to_file(scft_ctx *ctx, FILE *fp, const double *dev, long long n) {
+  const long long chunk = 1LL << 23;   // 64 MB of doubles
+  std::vector<double> buf((size_t)(n < chunk ? n : chunk));
+  for (long long o = 0; o < n; o += chunk) {
+    const long long k = n - o < chunk ? n - o : chunk;
+    cudaError_t e = cudaMemcpy(buf.data(), dev + o, sizeof(double) * k, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return scft_fail(ctx, SCFT_ERR_CUDA, cudaGetErrorString(e));
+    if (fwrite(buf.data(), sizeof(double), (size_t)k, fp) != (size_t)k)
+      return scft_fail(ctx, SCFT_ERR_IO, "checkpoint write failed");
+  }
+  return SCFT_OK;
+}
+int file_to_dev(scft_ctx *ctx, FILE *fp, double *dev, long long n) {
+  const long long chunk = 1LL << 23;
+  std::vector<double> buf((size_t)(n < chunk ? n : chunk));
+  for (long long o = 0; o < n; o += chunk) {
+    const long long k = n - o < chunk ? n - o : chunk;
+    if (fread(buf.data(), sizeof(double), (size_t)k, fp) != (size_t)k)
+      return scft_fail(ctx, SCFT_ERR_IO, "checkpoint file is short");
+    cudaError_t e = cudaMemcpy(dev + o, buf.data(), sizeof(double) * k, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return scft_fail(ctx, SCFT_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return SCFT_OK;
+}
+
+bool history_kept(const scft_ctx *ctx) {
+  return ctx->p.mixing == SCFT_MIX_ANDERSON && ctx->m1 > 0 &&
+         (int)ctx->hist_w.size() == ctx->m1 && ctx->gram != nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int scft_save_checkpoint(scft_ctx *ctx, const char *path, int with_history) {
+  if (!ctx || !path) return SCFT_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->p.device);
+  cudaError_t e = cudaStreamSynchronize(ctx->st);
+  if (e != cudaSuccess) return scft_fail(ctx, SCFT_ERR_CUDA, cudaGetErrorString(e));
+  const scft_params &p = ctx->p;
+  CkptHeader h;
+  memset(&h, 0, sizeof h);
+  memcpy(h.magic, "SCFTCKP1", 8);
+  h.version = 1;
+  h.nx = p.nx; h.ny = p.ny; h.nz = p.nz; h.batch = ctx->batch;
+  h.precision = p.precision; h.mixing = p.mixing; h.history = p.anderson_history;
+  h.has_history = (with_history && history_kept(ctx)) ? 1 : 0;
+  h.lx = p.lx; h.ly = p.ly; h.lz = p.lz; h.hAB = p.hAB; h.fA = p.fA; h.ds0 = p.ds0;
+  h.and_count = ctx->and_count;
+  FILE *fp = fopen(path, "wb");
+  if (!fp) return scft_fail(ctx, SCFT_ERR_IO, std::string("cannot write ") + path);
+  int rc = fwrite(&h, sizeof h, 1, fp) == 1 ? SCFT_OK
+                                             : scft_fail(ctx, SCFT_ERR_IO, "checkpoint write failed");
+  const long long BM = ctx->M * ctx->batch;
+  const double *fields[4] = {ctx->wa, ctx->wb, ctx->pha, ctx->phb};
+  for (int k = 0; k < 4 && rc == SCFT_OK; ++k) rc = dev_to_file(ctx, fp, fields[k], BM);
+  if (rc == SCFT_OK) rc = dev_to_file(ctx, fp, ctx->res, 4LL * ctx->batch);
+  if (rc == SCFT_OK && h.has_history) {
+    const int32_t m1 = ctx->m1;
+    if (fwrite(&m1, sizeof m1, 1, fp) != 1) rc = scft_fail(ctx, SCFT_ERR_IO, "checkpoint write failed");
+    for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = dev_to_file(ctx, fp, ctx->hist_w[j], 2 * BM);
+    for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = dev_to_file(ctx, fp, ctx->hist_d[j], 2 * BM);
+    if (rc == SCFT_OK) rc = dev_to_file(ctx, fp, ctx->gram, (long long)ctx->batch * m1 * m1);
+  }
+  if (fclose(fp) != 0 && rc == SCFT_OK) rc = scft_fail(ctx, SCFT_ERR_IO, "checkpoint close failed");
+  return rc;
+}
+
+int scft_load_checkpoint(scft_ctx *ctx, const char *path) {
+  if (!ctx || !path) return SCFT_ERR_INVALID_ARG;
+  FILE *fp = fopen(path, "rb");
+  if (!fp) return scft_fail(ctx, SCFT_ERR_IO, std::string("cannot open ") + path);
+  CkptHeader h;
+  if (fread(&h, sizeof h, 1, fp) != 1 || memcmp(h.magic, "SCFTCKP1", 8) != 0 || h.version != 1) {
+    fclose(fp);
+    return scft_fail(ctx, SCFT_ERR_IO, std::string("not a checkpoint file: ") + path);
+  }
+  const scft_params &p = ctx->p;
+  if (h.nx != p.nx || h.ny != p.ny || h.nz != p.nz || h.batch != ctx->batch) {
+    fclose(fp);
+    return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "checkpoint grid or batch differs from the context");
+  }
+  cudaSetDevice(ctx->p.device);
+  cudaError_t e = cudaStreamSynchronize(ctx->st);
+  if (e != cudaSuccess) {
+    fclose(fp);
+    return scft_fail(ctx, SCFT_ERR_CUDA, cudaGetErrorString(e));
+  }
+  const long long BM = ctx->M * ctx->batch;
+  double *fields[4] = {ctx->wa, ctx->wb, ctx->pha, ctx->phb};
+  int rc = SCFT_OK;
+  for (int k = 0; k < 4 && rc == SCFT_OK; ++k) rc = file_to_dev(ctx, fp, fields[k], BM);
+  if (rc == SCFT_OK) rc = file_to_dev(ctx, fp, ctx->res, 4LL * ctx->batch);
+  ctx->and_count = 0;
+  ctx->have_conc = false;   // the stored propagators belong to other fields
+  if (rc == SCFT_OK && h.has_history) {
+    int32_t m1 = 0;
+    const bool same = history_kept(ctx) && h.precision == p.precision &&
+                      h.mixing == p.mixing && h.history == p.anderson_history &&
+                      h.lx == p.lx && h.ly == p.ly && h.lz == p.lz && h.hAB == p.hAB &&
+                      h.fA == p.fA && h.ds0 == p.ds0;
+    if (fread(&m1, sizeof m1, 1, fp) != 1) rc = scft_fail(ctx, SCFT_ERR_IO, "checkpoint file is short");
+    if (rc == SCFT_OK && same && m1 == ctx->m1) {
+      for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = file_to_dev(ctx, fp, ctx->hist_w[j], 2 * BM);
+      for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = file_to_dev(ctx, fp, ctx->hist_d[j], 2 * BM);
+      if (rc == SCFT_OK) rc = file_to_dev(ctx, fp, ctx->gram, (long long)ctx->batch * m1 * m1);
+      if (rc == SCFT_OK) ctx->and_count = h.and_count;
+    }
+  }
+  fclose(fp);
+  return rc;
 }
 
 }  // extern "C"

@@ -91,6 +91,36 @@ def test_read_ab_txt_errors(pkg, tmp_path):
     assert e.value.status == pkg.ERR_IO
 
 
+AB7 = ("intag=1024\nxN=25.0\nfa=0.300\nlx=4.2, ly=7.2746, lz=2.0\n"
+       "Nx=128, Ny=128, Nz=64\nds0=0.005\nbatch=3\n")
+
+
+def test_read_ab_txt_optional_keys(pkg, tmp_path):
+    f = tmp_path / "ab.txt"
+    f.write_text(AB7 + "mixing=anderson\nhistory=30\nlambda=0.4\nstart=0.5\n"
+                 "wopt=0.02\nwcmp=0.2\nprecision=fp32\nNs=400\n\n")
+    p, tag = pkg.read_ab_txt(str(f))
+    assert tag == 1024 and (p.nx, p.nz, p.batch) == (128, 64, 3)
+    assert p.mixing == pkg.MIX_ANDERSON and p.anderson_history == 30
+    assert (p.anderson_lambda, p.anderson_start, p.wopt, p.wcmp) == (0.4, 0.5, 0.02, 0.2)
+    assert p.precision == pkg.PREC_FP32 and p.ds0 == 1.0 / 400
+    # without the optional lines: the reference's defaults
+    f.write_text(AB7)
+    p, _ = pkg.read_ab_txt(str(f))
+    assert p.mixing == pkg.MIX_SIMPLE and p.precision == pkg.PREC_FP64
+    assert (p.wopt, p.wcmp, p.ds0) == (0.05, 0.10, 0.005)
+
+
+@pytest.mark.parametrize("extra", ["mixing=broyden\n", "history=lots\n", "colour=blue\n",
+                                   "just text\n", "Ns=0\n"])
+def test_read_ab_txt_rejects_bad_optional_keys(pkg, tmp_path, extra):
+    f = tmp_path / "ab.txt"
+    f.write_text(AB7 + extra)
+    with pytest.raises(pkg.ScftError) as e:
+        pkg.read_ab_txt(str(f))
+    assert e.value.status == pkg.ERR_IO
+
+
 def test_params_layout_matches_header(pkg, tmp_path):
     import shutil
     import subprocess

@@ -1,0 +1,126 @@
+"""Binary FP64 checkpoint (exact resume) and JSON-lines progress metrics.
+
+A run saved after k iterations and resumed in a fresh context must repeat
+the uninterrupted run bit for bit, with simple mixing and with Anderson
+mixing (whose history ring, Gram matrix and iteration count are part of the
+state)."""
+import json
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+G = dict(nx=32, ny=32, nz=16, lx=3.8, ly=3.8, lz=1.9, hAB=18.0, fA=0.36, ds0=0.01)
+
+
+def start_fields(batch=2):
+    from scft_gb300 import fields as fl
+    return fl.gyroid(G["nx"], G["ny"], G["nz"], G["lx"], G["ly"], G["lz"], G["hAB"], seed=3,
+                     batch=batch)
+
+
+def ctx_kw(pkg, prec, mixing, **extra):
+    kw = dict(G, batch=2, precision=pkg.PREC_FP32 if prec == "fp32" else pkg.PREC_FP64)
+    if mixing == "anderson":
+        kw.update(mixing=pkg.MIX_ANDERSON, anderson_history=5, anderson_start=1e9)
+    kw.update(extra)
+    return kw
+
+
+@pytest.mark.parametrize("mixing", ["simple", "anderson"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_resume_repeats_the_run_bit_for_bit(pkg, tmp_path, prec, mixing):
+    wa, wb = start_fields()
+    path = tmp_path / "run.ckpt"
+    kw = ctx_kw(pkg, prec, mixing)
+    with pkg.Context(**kw) as a:
+        a.set_w(wa, wb)
+        a.iterate(12)                 # Anderson: the 6-slot ring has wrapped
+        a.save_checkpoint(path)
+        a.iterate(9)
+        ref = [a.wa, a.wb, a.pha, a.phb, a.residual()[0], a.free_energy()]
+    with pkg.Context(**kw) as b:
+        b.load_checkpoint(path)
+        b.iterate(9)
+        got = [b.wa, b.wb, b.pha, b.phb, b.residual()[0], b.free_energy()]
+    for r, g in zip(ref, got):
+        assert np.array_equal(r, g)
+
+
+def test_history_restarts_when_the_operator_differs(pkg, tmp_path):
+    wa, wb = start_fields()
+    path = tmp_path / "run.ckpt"
+    with pkg.Context(**ctx_kw(pkg, "fp64", "anderson")) as a:
+        a.set_w(wa, wb)
+        a.iterate(8)
+        a.save_checkpoint(path)
+        w_saved = (a.wa, a.wb, a.pha)
+    # another chi N: the fields load, the history (of the other operator) does not
+    with pkg.Context(**ctx_kw(pkg, "fp64", "anderson", hAB=17.5)) as b:
+        b.load_checkpoint(path)
+        assert np.array_equal(b.wa, w_saved[0]) and np.array_equal(b.pha, w_saved[2])
+        b.iterate(3)
+        assert np.isfinite(b.residual()[0]).all()
+    # fields only (no history in the file) into a simple-mixing context
+    with pkg.Context(**ctx_kw(pkg, "fp64", "anderson")) as a:
+        a.set_w(wa, wb)
+        a.iterate(2)
+        a.save_checkpoint(path, with_history=False)
+        w2 = a.wb
+    with pkg.Context(**ctx_kw(pkg, "fp32", "simple")) as c:
+        c.load_checkpoint(path)
+        assert np.array_equal(c.wb, w2)
+
+
+def test_checkpoint_errors(pkg, tmp_path):
+    wa, wb = start_fields()
+    path = tmp_path / "run.ckpt"
+    with pkg.Context(**ctx_kw(pkg, "fp64", "simple")) as a:
+        a.set_w(wa, wb)
+        a.save_checkpoint(path)
+    with pkg.Context(**dict(ctx_kw(pkg, "fp64", "simple"), nz=8, lz=0.95)) as b:
+        with pytest.raises(pkg.ScftError) as e:
+            b.load_checkpoint(path)
+        assert e.value.status == pkg.ERR_INVALID_ARG
+        bad = tmp_path / "bad.ckpt"
+        bad.write_bytes(b"not a checkpoint at all")
+        with pytest.raises(pkg.ScftError) as e:
+            b.load_checkpoint(bad)
+        assert e.value.status == pkg.ERR_IO
+        with pytest.raises(pkg.ScftError) as e:
+            b.load_checkpoint(tmp_path / "missing.ckpt")
+        assert e.value.status == pkg.ERR_IO
+    # a truncated file: the fields are short
+    data = path.read_bytes()
+    short = tmp_path / "short.ckpt"
+    short.write_bytes(data[: len(data) // 2])
+    with pkg.Context(**ctx_kw(pkg, "fp64", "simple")) as c:
+        with pytest.raises(pkg.ScftError) as e:
+            c.load_checkpoint(short)
+        assert e.value.status == pkg.ERR_IO
+
+
+def test_free_writes_json_lines(pkg, tmp_path, capfd):
+    wa, wb = start_fields()
+    path = tmp_path / "metrics.jsonl"
+    with pkg.Context(**ctx_kw(pkg, "fp64", "simple")) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.set_metrics_file(str(path))
+        ctx.free(20, 10)
+        fe = ctx.free_energy()
+        mx, rms = ctx.residual()
+        ctx.set_metrics_file(None)
+        ctx.free(10, 10)              # off again: nothing appended
+    rows = [json.loads(line) for line in path.read_text().splitlines()]
+    assert [(r["iteration"], r["instance"]) for r in rows] == [(10, 0), (10, 1), (20, 0), (20, 1)]
+    keys = {"F", "F_AB", "F_W", "F_S", "inCompMax", "residual_max", "residual_rms", "elapsed_s"}
+    assert all(keys <= set(r) for r in rows)
+    for i in range(2):
+        last = rows[2 + i]
+        np.testing.assert_allclose([last["F"], last["F_AB"], last["F_W"], last["F_S"],
+                                    last["inCompMax"]], fe[i], rtol=1e-14, atol=1e-15)
+        assert last["residual_max"] == mx[i] and last["residual_rms"] == rms[i]
+    assert rows[2]["elapsed_s"] >= rows[0]["elapsed_s"] >= 0
+    out = capfd.readouterr().out     # the reference's progress lines are unchanged
+    assert out.count("GPU 0 batch 0:") == 3
