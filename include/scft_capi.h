@@ -90,6 +90,11 @@ typedef struct scft_params {
 #define SCFT_FLAG_AUTOTUNE 32     /* time every legal schedule at creation and keep the fastest */
 #define SCFT_FLAG_NO_FUSED_STEPS 64 /* two-stream chains: two launches per contour step instead of
                                        one fused kernel per step pair (k_zz / k_xyxy) */
+#define SCFT_FLAG_SIMPSON 128     /* phi contour sums with Simpson weights instead of the
+                                     reference's trapezoid (w_to_phi_go, cuda_aid.cu:87-107):
+                                     composite 1/3 rule, the 3/8 rule over the last three steps
+                                     of a block with an odd step count; the adjoint and the
+                                     stress use the same weights */
 
 /* Fill *p with the reference defaults (32^3, box 4, xN 20, fa 0.5,
  * ds0 0.01, batch 1, FP64, simple mixing wopt 0.05 wcmp 0.10). */

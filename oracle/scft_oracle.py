@@ -54,6 +54,7 @@ class Params:
     wopt: float = 0.05
     wcmp: float = 0.10
     aver_it: int = 10
+    simpson: bool = False      # contour sums with Simpson weights (no reference counterpart)
 
     @property
     def shape(self):
@@ -213,6 +214,42 @@ class Conc:
     wa: np.ndarray           # wa after getConc's own average_value (cuda_scft.cu:71)
 
 
+def contour_weights(n: int, simpson: bool = False) -> np.ndarray:
+    """Weights of the contour points s = 0..n of a block of n steps.
+
+    Trapezoid (``w_to_phi_go``, cuda_aid.cu:87-107): 1/2 at both ends, 1
+    inside; the n == 0 block has the single weight 1/2 (cuda_aid.cu:91).
+    Simpson (an option without a reference counterpart): the composite 1/3
+    rule for even n; for odd n >= 3 the 1/3 rule over the first n-3 steps and
+    the 3/8 rule over the last three; n == 1 stays trapezoid.  The weights of
+    a block with n >= 1 sum to n."""
+    if n == 0:
+        return np.array([0.5])
+    if not simpson or n == 1:
+        w = np.ones(n + 1)
+        w[0] = w[-1] = 0.5
+        return w
+    m = n if n % 2 == 0 else n - 3
+    w = np.zeros(n + 1)
+    if m > 0:
+        w[1:m:2] = 4.0 / 3.0
+        w[2:m:2] = 2.0 / 3.0
+        w[0] += 1.0 / 3.0
+        w[m] += 1.0 / 3.0
+    if m < n:
+        w[m] += 3.0 / 8.0
+        w[m + 1] += 9.0 / 8.0
+        w[m + 2] += 9.0 / 8.0
+        w[n] += 3.0 / 8.0
+    return w
+
+
+def contour_sum(q: np.ndarray, qc: np.ndarray, simpson: bool = False) -> np.ndarray:
+    """sum_s w_s q(s) qc(s) over a block, ``q``/``qc``: ``[batch][ns+1][...]``."""
+    w = contour_weights(q.shape[1] - 1, simpson)
+    return np.tensordot(w, np.moveaxis(q * qc, 1, 0), axes=1)
+
+
 def trapezoid_sum(q: np.ndarray, qc: np.ndarray) -> np.ndarray:
     """Contour sum of ``w_to_phi_go`` (cuda_aid.cu:87-107): weights 1/2 at both
     ends, 1 inside.  ``q``/``qc``: ``[batch][ns+1][...]``."""
@@ -239,8 +276,12 @@ def get_conc(wa: np.ndarray, wb: np.ndarray, p: Params, kdz_half=None) -> Conc:
     ql = qb[:, p.dNsB].reshape(b, -1).sum(axis=1)             # cal_ql, :118
     Q = ql / p.M                                              # :124
     ffl = p.ds0 / Q                                           # :125
-    pha = ffl[:, None, None, None] * trapezoid_sum(qa, qca)   # w_to_phi_go, :130
-    phb = ffl[:, None, None, None] * trapezoid_sum(qb, qcb)
+    if p.simpson:
+        pha = ffl[:, None, None, None] * contour_sum(qa, qca, True)
+        phb = ffl[:, None, None, None] * contour_sum(qb, qcb, True)
+    else:
+        pha = ffl[:, None, None, None] * trapezoid_sum(qa, qca)   # w_to_phi_go, :130
+        phb = ffl[:, None, None, None] * trapezoid_sum(qb, qcb)
     return Conc(pha, phb, Q, qa, qcb, qb, qca, wa)
 
 

@@ -47,7 +47,7 @@ EXPORTS = [
     "scft_spline_deriv", "scft_spline_integral", "scft_spline_eval_device",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
-FLAG_AUTOTUNE, FLAG_NO_FUSED_STEPS = 32, 64
+FLAG_AUTOTUNE, FLAG_NO_FUSED_STEPS, FLAG_SIMPSON = 32, 64, 128
 
 
 class ScftParams(C.Structure):

@@ -8,7 +8,8 @@
 // split step A_s = W K W, W = exp(-w ds/2) of the block's field and K the
 // diffusion filter exp(-ds k^2).  K is real, even and circulant, so A_s is
 // symmetric and its adjoint is A_s itself.  Q = <q(N)>,
-// phiA/B = (ds/Q) * trapezoid sums of q q+ over the block's contour points.
+// phiA/B = (ds/Q) * contour sums (trapezoid or Simpson weights) of q q+ over
+// the block's contour points.
 //
 // Box derivative of one step: dA_s/dL_a = W (dK/dL_a) W, where dK/dL_a is K
 // with the axis-a gain multiplied by 2 ds k_a^2 / L_a (k_a ~ 1/L_a), or, for
@@ -109,7 +110,7 @@ __global__ void k_sum_slots(const double *__restrict__ partial, int nblk, double
 }
 
 // adjoint seed at one contour point: out = ffl (cA phibarA + cB phibarB) * v
-// (v == null: 1), and the point's trapezoid terms of phi: S += c q q+
+// (v == null: 1), and the point's contour-weight terms of phi: S += c q q+
 template <typename R>
 __global__ void k_seed(R *__restrict__ out, const R *__restrict__ v, long long v_bs,
                        const double *__restrict__ pbA, const double *__restrict__ pbB, double cA,
@@ -188,9 +189,6 @@ __global__ void k_axpy_inst(double *__restrict__ wbar, const double *__restrict_
     wbar[b * M + i] += coef[b] * G[b * M + i];
 }
 
-// trapezoid weight of contour point s of a block of n steps (the ns = 0
-// block has the single weight 1/2, as the reference's loop gives)
-double trap_w(int s, int n) { return (s == 0 || s == n) ? 0.5 : 1.0; }
 
 }  // namespace
 
@@ -228,10 +226,12 @@ enum AccKind { ACC_L1 = 0, ACC_Q = 3, ACC_L2 = 6, ACC_U1 = 9, ACC_UQ = 10, ACC_U
 
 int field_of_step(const scft_ctx *ctx, int s) { return s <= ctx->NsA ? 0 : 1; }
 
-// trapezoid weights of contour point s in the A and B blocks
+// contour weights of point s in the A and B blocks (those of the forward
+// contour sums: trapezoid, or Simpson with SCFT_FLAG_SIMPSON)
 void weights(const scft_ctx *ctx, int s, double *cA, double *cB) {
-  *cA = s <= ctx->NsA ? trap_w(s, ctx->NsA) : 0.0;
-  *cB = s >= ctx->NsA ? trap_w(s - ctx->NsA, ctx->dNsB) : 0.0;
+  const bool simpson = (ctx->p.flags & SCFT_FLAG_SIMPSON) != 0;
+  *cA = s <= ctx->NsA ? scft::contour_weight(s, ctx->NsA, simpson) : 0.0;
+  *cB = s >= ctx->NsA ? scft::contour_weight(s - ctx->NsA, ctx->dNsB, simpson) : 0.0;
 }
 
 int ensure_adjoint(scft_ctx *ctx, int K) {

@@ -514,12 +514,13 @@ int q_and_phi(scft_ctx *ctx) {
   CKL(scft::launch_finalize_sum(ctx->partial, ctx->nblk, B, 1.0, ctx->sum, ctx->st));
   CKL(scft::launch_q_ffl(ctx->sum, M, ctx->p.ds0, B, ctx->Q, ctx->ffl, ctx->st));
   // w_to_phi_go (cuda_scft.cu:130)
+  const bool simpson = (ctx->p.flags & SCFT_FLAG_SIMPSON) != 0;
   CKL(scft::launch_contour_phi<R>(static_cast<const R *>(ctx->q[SCFT_Q_A]),
                                   static_cast<const R *>(ctx->q[SCFT_Q_CA]), ctx->NsA, M, B,
-                                  ctx->ffl, ctx->pha, ctx->st));
+                                  ctx->ffl, ctx->pha, simpson, ctx->st));
   CKL(scft::launch_contour_phi<R>(static_cast<const R *>(ctx->q[SCFT_Q_B]),
                                   static_cast<const R *>(ctx->q[SCFT_Q_CB]), ctx->dNsB, M, B,
-                                  ctx->ffl, ctx->phb, ctx->st));
+                                  ctx->ffl, ctx->phb, simpson, ctx->st));
   return SCFT_OK;
 }
 
@@ -839,7 +840,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     if (p.reserved[i]) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "reserved fields must be 0");
   if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_PIPE | SCFT_FLAG_TWO_STREAMS |
                   SCFT_FLAG_LOCKSTEP | SCFT_FLAG_NO_XY | SCFT_FLAG_AUTOTUNE |
-                  SCFT_FLAG_NO_FUSED_STEPS))
+                  SCFT_FLAG_NO_FUSED_STEPS | SCFT_FLAG_SIMPSON))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad flags");
   if (!(p.lx > 0 && p.ly > 0 && p.lz > 0 && p.ds0 > 0 && p.fA >= 0 && p.fA <= 1 && p.batch >= 1))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");

@@ -3,6 +3,8 @@
 // energy), the trapezoid contour sum giving phi, and simple mixing.
 // All reductions are two-level and in a fixed order, so results are
 // bit-reproducible from run to run.
+#include <string.h>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -116,24 +118,39 @@ __global__ void k_q_ffl(const double *__restrict__ sum, long long M, double ds0,
 // contour-outer [b][s][M].  FP64 accumulation for double; for float the
 // products are accumulated with a compensated (TwoSum) FP32 pair, which keeps
 // ~FP64-level summation error without GB300's slow FP64 pipe.
+// cw: the block's contour weights (contour_weights below); the reference's
+// trapezoid is m = ns, c_odd = c_even = 1 and the ends listed with 1/2.
 template <typename R>
 __global__ void k_contour_phi(const R *__restrict__ q, const R *__restrict__ qc, int ns,
                               long long M, const double *__restrict__ ffl,
-                              double *__restrict__ phi);
+                              double *__restrict__ phi, ContourWeights cw);
 
 template <>
 __global__ void k_contour_phi<double>(const double *__restrict__ q, const double *__restrict__ qc,
                                       int ns, long long M, const double *__restrict__ ffl,
-                                      double *__restrict__ phi) {
+                                      double *__restrict__ phi, ContourWeights cw) {
   const int b = blockIdx.y;
   const long long qbs = (long long)(ns + 1) * M;
   const double *qb = q + b * qbs, *qcb = qc + b * qbs;
+  const bool trap = cw.c_odd == 1.0 && cw.c_even == 1.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
        i += (long long)gridDim.x * blockDim.x) {
-    // ns == 0: the single end point gets weight 1/2 (cuda_aid.cu:91)
-    double acc = 0.5 * qb[i] * qcb[i];
-    for (int s = 1; s < ns; ++s) acc += qb[s * M + i] * qcb[s * M + i];
-    if (ns > 0) acc += 0.5 * qb[ns * M + i] * qcb[ns * M + i];
+    // special points before the interior (s = 0), in the reference's order
+    double acc = 0.0;
+    int k = 0;
+    for (; k < cw.nspec && cw.s[k] < 1; ++k) acc += cw.w[k] * qb[cw.s[k] * M + i] * qcb[cw.s[k] * M + i];
+    if (trap) {
+      for (int s = 1; s < cw.m; ++s) acc += qb[s * M + i] * qcb[s * M + i];
+    } else {
+      double ao = 0.0, ae = 0.0;
+      for (int s = 1; s < cw.m; ++s) {
+        const double pr = qb[s * M + i] * qcb[s * M + i];
+        if (s & 1) ao += pr;
+        else ae += pr;
+      }
+      acc += cw.c_odd * ao + cw.c_even * ae;
+    }
+    for (; k < cw.nspec; ++k) acc += cw.w[k] * qb[cw.s[k] * M + i] * qcb[cw.s[k] * M + i];
     phi[b * M + i] = acc * ffl[b];
   }
 }
@@ -141,22 +158,43 @@ __global__ void k_contour_phi<double>(const double *__restrict__ q, const double
 template <>
 __global__ void k_contour_phi<float>(const float *__restrict__ q, const float *__restrict__ qc,
                                      int ns, long long M, const double *__restrict__ ffl,
-                                     double *__restrict__ phi) {
+                                     double *__restrict__ phi, ContourWeights cw) {
   const int b = blockIdx.y;
   const long long qbs = (long long)(ns + 1) * M;
   const float *qb = q + b * qbs, *qcb = qc + b * qbs;
+  const bool trap = cw.c_odd == 1.0 && cw.c_even == 1.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
        i += (long long)gridDim.x * blockDim.x) {
-    float hi = 0.f, lo = 0.f;
-    for (int s = 1; s < ns; ++s) {
-      const float p = qb[s * M + i] * qcb[s * M + i];
-      float e;
-      two_sum(hi, p, hi, e);
-      lo += e;
+    // interior: compensated FP32 sums, one per weight class
+    float hi = 0.f, lo = 0.f, hi2 = 0.f, lo2 = 0.f;
+    if (trap) {
+      for (int s = 1; s < cw.m; ++s) {
+        const float p = qb[s * M + i] * qcb[s * M + i];
+        float e;
+        two_sum(hi, p, hi, e);
+        lo += e;
+      }
+    } else {
+      for (int s = 1; s < cw.m; ++s) {
+        const float p = qb[s * M + i] * qcb[s * M + i];
+        float e;
+        if (s & 1) {
+          two_sum(hi, p, hi, e);
+          lo += e;
+        } else {
+          two_sum(hi2, p, hi2, e);
+          lo2 += e;
+        }
+      }
     }
-    const double ends = ns > 0 ? 0.5 * ((double)qb[i] * qcb[i] + (double)qb[ns * M + i] * qcb[ns * M + i])
-                               : 0.5 * (double)qb[i] * qcb[i];
-    phi[b * M + i] = ((double)hi + (double)lo + ends) * ffl[b];
+    // the listed points in FP64
+    double ends = 0.0;
+    for (int k = 0; k < cw.nspec; ++k)
+      ends += cw.w[k] * ((double)qb[cw.s[k] * M + i] * (double)qcb[cw.s[k] * M + i]);
+    const double inner = trap ? (double)hi + (double)lo
+                              : cw.c_odd * ((double)hi + (double)lo) +
+                                    cw.c_even * ((double)hi2 + (double)lo2);
+    phi[b * M + i] = (inner + ends) * ffl[b];
   }
 }
 
@@ -357,10 +395,58 @@ cudaError_t launch_q_ffl(const double *sum, long long M, double ds0, int batch, 
   k_q_ffl<<<(batch + 127) / 128, 128, 0, st>>>(sum, M, ds0, batch, Q, ffl);
   return cudaGetLastError();
 }
+double contour_weight(int s, int n, bool simpson) {
+  if (s < 0 || s > n) return 0.0;
+  if (n == 0) return 0.5;                                 // cuda_aid.cu:91
+  if (!simpson || n == 1) return (s == 0 || s == n) ? 0.5 : 1.0;
+  const int m = (n % 2 == 0) ? n : n - 3;                 // end of the 1/3 rule
+  double w = 0.0;
+  if (m > 0 && s <= m) w += (s == 0 || s == m) ? 1.0 / 3.0 : ((s & 1) ? 4.0 / 3.0 : 2.0 / 3.0);
+  if (m < n && s >= m) w += (s == m || s == n) ? 3.0 / 8.0 : 9.0 / 8.0;   // the 3/8 rule
+  return w;
+}
+
+ContourWeights contour_weights(int n, bool simpson) {
+  ContourWeights cw;
+  memset(&cw, 0, sizeof cw);
+  cw.c_odd = cw.c_even = 1.0;
+  if (n == 0) {
+    cw.m = 0;
+    cw.nspec = 1;
+    cw.s[0] = 0;
+    cw.w[0] = 0.5;
+    return cw;
+  }
+  if (!simpson || n == 1) {
+    cw.m = n;
+    cw.nspec = 2;
+    cw.s[0] = 0; cw.w[0] = 0.5;
+    cw.s[1] = n; cw.w[1] = 0.5;
+    return cw;
+  }
+  const int m = (n % 2 == 0) ? n : n - 3;
+  cw.c_odd = 4.0 / 3.0;
+  cw.c_even = 2.0 / 3.0;
+  cw.m = m > 0 ? m : 1;                                   // interior 1..m-1
+  int k = 0;
+  for (int s = 0; s <= n; ++s) {
+    const bool interior = s >= 1 && s < cw.m;
+    if (!interior) {
+      cw.s[k] = s;
+      cw.w[k] = contour_weight(s, n, true);
+      ++k;
+    }
+  }
+  cw.nspec = k;
+  return cw;
+}
+
 template <typename R>
 cudaError_t launch_contour_phi(const R *q, const R *qc, int ns, long long M, int batch,
-                               const double *ffl, double *phi, cudaStream_t st) {
-  k_contour_phi<R><<<dim3(grid_for(M), batch), kThreads, 0, st>>>(q, qc, ns, M, ffl, phi);
+                               const double *ffl, double *phi, bool simpson, cudaStream_t st) {
+  const ContourWeights cw = contour_weights(ns, simpson);
+  if (cw.nspec > 5) return cudaErrorInvalidValue;
+  k_contour_phi<R><<<dim3(grid_for(M), batch), kThreads, 0, st>>>(q, qc, ns, M, ffl, phi, cw);
   return cudaGetLastError();
 }
 cudaError_t launch_phi_w(double *wa, double *wb, const double *pha, const double *phb,
@@ -418,7 +504,7 @@ cudaError_t launch_free_energy_finalize(const double *partial, int nblk, int bat
   template cudaError_t launch_partial_sum<R>(const R *, long long, long long, int, double *, int, \
                                              cudaStream_t);                                       \
   template cudaError_t launch_contour_phi<R>(const R *, const R *, int, long long, int,           \
-                                             const double *, double *, cudaStream_t);
+                                             const double *, double *, bool, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

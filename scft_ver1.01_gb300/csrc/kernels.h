@@ -131,10 +131,24 @@ cudaError_t launch_minus_average(double *data, const double *sum, long long M, i
 // Q = sum/M ; ffl = ds0/Q  (cal_ql + host lines of getConc)
 cudaError_t launch_q_ffl(const double *sum, long long M, double ds0, int batch, double *Q,
                          double *ffl, cudaStream_t st);
-// phi = ffl * trapezoid contour sum of q*qc  (w_to_phi_go)
+// Weight of contour point s (0..n) of a block of n steps: the reference's
+// trapezoid (1/2 at both ends, 1 inside; the n == 0 block has the single
+// weight 1/2, cuda_aid.cu:87-107), or Simpson (1/3 rule; for odd n >= 3 the
+// 3/8 rule over the last three steps; n == 1 stays trapezoid).
+double contour_weight(int s, int n, bool simpson);
+// The same weights in kernel form: interior points 1..m-1 take c_odd (odd s)
+// or c_even (even s); up to five listed points take their own weight.
+struct ContourWeights {
+  int m, nspec;
+  double c_odd, c_even;
+  int s[5];
+  double w[5];
+};
+ContourWeights contour_weights(int n, bool simpson);
+// phi = ffl * contour sum of q*qc with the weights above (w_to_phi_go)
 template <typename R>
 cudaError_t launch_contour_phi(const R *q, const R *qc, int ns, long long M, int batch,
-                               const double *ffl, double *phi, cudaStream_t st);
+                               const double *ffl, double *phi, bool simpson, cudaStream_t st);
 // simple mixing (phi_w); writes the residual max-norm partials if resid != null
 cudaError_t launch_phi_w(double *wa, double *wb, const double *pha, const double *phb,
                          double hAB, double wopt, double wcmp, long long M, int batch,

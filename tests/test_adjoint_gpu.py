@@ -86,6 +86,34 @@ def test_adjoint_matches_finite_differences(pkg, orc, case):
         assert abs(ad - fd) < 2e-6 * max(abs(fd), 1e-3), (a, ad, fd)
 
 
+@pytest.mark.parametrize("fA", [0.4, 0.35])     # blocks of 8/12 and 7/13 steps
+def test_adjoint_with_simpson_weights(pkg, orc, fA):
+    """SCFT_FLAG_SIMPSON: the adjoint differentiates the Simpson-weighted
+    contour sums (central differences of the oracle's functional)."""
+    case = CASES[0][:6] + (fA, 0.05)
+    ctx, p = make(pkg, orc, case, flags=pkg.FLAG_SIMPSON)
+    p.simpson = True
+    rng = np.random.default_rng(11)
+    wa, wb = fields(p.shape, 2, 6)
+    pbA = rng.normal(0, 1, wa.shape)
+    pbB = rng.normal(0, 1, wa.shape)
+    Qb = rng.normal(0, 1, 2)
+    with ctx:
+        ctx.set_w(wa, wb)
+        gA, gB, gL = ctx.adjoint(pbA, pbB, Qb)
+    J = lambda a, b, pp: orc.conc_functional(a, b, pp, pbA, pbB, Qb)
+    dA = rng.normal(0, 1, wa.shape)
+    dB = rng.normal(0, 1, wa.shape)
+    h = 1e-5
+    fd = (J(wa + h * dA, wb + h * dB, p) - J(wa - h * dA, wb - h * dB, p)) / (2 * h)
+    ad = float((gA * dA).sum() + (gB * dB).sum())
+    assert abs(ad - fd) < 2e-6 * max(abs(fd), 1e-3), (ad, fd)
+    h = 1e-4 * p.lx
+    fd = (J(wa, wb, orc.with_box(p, p.lx + h, p.ly, p.lz))
+          - J(wa, wb, orc.with_box(p, p.lx - h, p.ly, p.lz))) / (2 * h)
+    assert abs(float(gL[:, 0].sum()) - fd) < 2e-6 * max(abs(fd), 1e-3)
+
+
 def test_dlnQ_dw_is_minus_phi_over_M(pkg, orc):
     ctx, p = make(pkg, orc, CASES[0])
     with ctx:

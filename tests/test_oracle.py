@@ -199,3 +199,20 @@ def test_analytic_stress_matches_finite_differences(orc):
         a = orc.stress_spectral(wa, wb, p)
         b = orc.stress_fd(wa, wb, p)
         assert np.abs(a - b).max() < 1e-7 * np.abs(a).max()
+
+
+def test_contour_weights(orc):
+    """Trapezoid weights are the reference's (w_to_phi_go, cuda_aid.cu:87-107);
+    the Simpson weights of a block of n >= 1 steps sum to n and integrate
+    cubics exactly (the 1/3 rule and, for odd n, the 3/8 rule at the end)."""
+    assert list(orc.contour_weights(0)) == [0.5] == list(orc.contour_weights(0, True))
+    assert list(orc.contour_weights(4)) == [0.5, 1, 1, 1, 0.5]
+    assert list(orc.contour_weights(1, True)) == [0.5, 0.5]
+    for n in range(2, 40):
+        w = orc.contour_weights(n, True)
+        s = np.arange(n + 1.0)
+        for k in range(4):
+            assert abs((w * s ** k).sum() - n ** (k + 1) / (k + 1)) < 1e-12 * n ** (k + 1)
+    rng = np.random.default_rng(0)
+    q, qc = rng.random((2, 2, 8, 3, 4))
+    np.testing.assert_allclose(orc.contour_sum(q, qc), orc.trapezoid_sum(q, qc), rtol=1e-15)

@@ -82,6 +82,45 @@ def test_get_conc_parity(pkg, orc, g, prec):
         assert rel(ctx.get_q(pkg.Q_CA, 0), ref.qca[:, 0]) < TOL[prec]
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("g,fA,ds0", [
+    (GRIDS[1], 0.45, 0.01),    # NsA 45, dNsB 55: the 3/8 rule closes both blocks
+    (GRIDS[7], 0.5, 0.01),     # 50 / 50: the 1/3 rule alone
+    (GRIDS[0], 0.75, 0.25),    # 3 / 1: the 3/8 rule alone, and a one-step block
+    (GRIDS[8], 0.36, 0.005),   # 72 / 128 on the fused-step kernels
+])
+def test_simpson_contour_parity(pkg, orc, g, fA, ds0, prec):
+    """SCFT_FLAG_SIMPSON: phi from Simpson-weighted contour sums (an option;
+    the reference integrates with the trapezoid rule)."""
+    from scft_gb300 import fields
+    kw = dict(hAB=20.0, fA=fA, ds0=ds0)
+    p = oparams(orc, g, simpson=True, **kw)
+    wa, wb = fields.lamellar(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 20.0, seed=2, batch=2)
+    ref = orc.get_conc(wa, wb, p)
+    trap = orc.get_conc(wa, wb, oparams(orc, g, **kw))
+    with make_ctx(pkg, g, prec, flags=pkg.FLAG_SIMPSON, **kw) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.get_conc()
+        assert rel(ctx.pha, ref.pha) < TOL[prec]
+        assert rel(ctx.phb, ref.phb) < TOL[prec]
+        assert np.abs(ctx.Q() / ref.Q - 1).max() < TOL[prec]
+    # the option changes phi (by far more than the FP64 tolerance), not Q
+    assert rel(ref.pha, trap.pha) > 1e4 * TOL[0]
+    assert np.array_equal(ref.Q, trap.Q)
+
+
+def test_simpson_uniform_field_gives_the_block_fractions(pkg):
+    """w = 0: q = 1, Q = 1 and phiA = ds * (sum of the A block's weights) = fA
+    for either rule (the weights of a block of n steps sum to n)."""
+    for flags in (0, pkg.FLAG_SIMPSON):
+        with pkg.Context(nx=16, ny=16, nz=8, fA=0.35, ds0=0.05, flags=flags) as ctx:
+            z = np.zeros(ctx.shape)
+            ctx.set_w(z, z)
+            ctx.get_conc()
+            np.testing.assert_allclose(ctx.pha, 0.35, rtol=1e-13)
+            np.testing.assert_allclose(ctx.phb, 0.65, rtol=1e-13)
+
+
 def test_average_value_and_phi_w(pkg, orc):
     g = GRIDS[1]
     p = oparams(orc, g, hAB=15.0)
