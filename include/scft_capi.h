@@ -38,6 +38,11 @@ extern "C" {
 /* ---- enums ---- */
 #define SCFT_PREC_FP64 0          /* plain path: propagation and FFTs in FP64 */
 #define SCFT_PREC_FP32 1          /* FP32 propagation, FP64 Q / contour sums / F / mixing */
+#define SCFT_PREC_DF 2            /* propagation in double-float arithmetic (pairs of FP32
+                                     numbers, ~48 significant bits) on the FP32 pipe, FP64
+                                     elsewhere: FP64-level results faster than native FP64 on
+                                     GB300; Nx of 64 or 128, Ny and Nz of 1, 32, 64 or 128,
+                                     Ny*Nz a multiple of 64; no adjoint or stress */
 
 #define SCFT_FIELD_WA 0
 #define SCFT_FIELD_WB 1

@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(HERE, "libscft_gb300.so")
 OK = 0
 ERR_INVALID_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NO_MEMORY = 1, 2, 3, 4
 ERR_NOT_FINITE, ERR_IO, ERR_NO_DEVICE = 5, 6, 7
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_DF = 0, 1, 2
 FIELD_WA, FIELD_WB, FIELD_PHA, FIELD_PHB = 0, 1, 2, 3
 Q_A, Q_CB, Q_B, Q_CA = 0, 1, 2, 3
 MIX_SIMPLE, MIX_ANDERSON, MIX_CONSTRAINED, MIX_CONSTRAINED_EX = 0, 1, 2, 3

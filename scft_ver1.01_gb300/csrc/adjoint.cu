@@ -564,6 +564,8 @@ int scft_adjoint(scft_ctx *ctx, const double *pha_bar, const double *phb_bar,
                  const double *Q_bar, double *wa_bar, double *wb_bar, double *L_bar,
                  int checkpoint_every) {
   if (!ctx) return SCFT_ERR_INVALID_ARG;
+  if (ctx->rkind == kRealDF)
+    return scft_fail(ctx, SCFT_ERR_UNSUPPORTED, "no adjoint for double-float contexts");
   const int N = ctx->NsA + ctx->dNsB;
   if (N < 1) return scft_fail(ctx, SCFT_ERR_UNSUPPORTED, "adjoint needs at least one step");
   if (checkpoint_every < 0) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad checkpoint interval");
@@ -591,6 +593,8 @@ int scft_adjoint_checkpoints(scft_ctx *ctx, int checkpoint_every, int *slices,
 
 int scft_stress(scft_ctx *ctx, double *dF_dL) {
   if (!ctx || !dF_dL) return SCFT_ERR_INVALID_ARG;
+  if (ctx->rkind == kRealDF)
+    return scft_fail(ctx, SCFT_ERR_UNSUPPORTED, "no stress for double-float contexts");
   if (!ctx->have_conc)
     return scft_fail(ctx, SCFT_ERR_INVALID_ARG,
                      "no getConc at the current box: call scft_get_conc first");

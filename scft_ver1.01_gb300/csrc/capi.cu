@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "ctx.h"
@@ -86,6 +87,10 @@ int upload_gains(scft_ctx *ctx) {
       std::vector<float> gf(g.begin(), g.end()), dgf(dg.begin(), dg.end());
       CK(cudaMemcpy(const_cast<void *>(ap.gain), gf.data(), 4 * ap.n, cudaMemcpyHostToDevice));
       CK(cudaMemcpy(dptr, dgf.data(), 4 * ap.n, cudaMemcpyHostToDevice));
+    } else if (ctx->rkind == kRealDF) {
+      std::vector<scft::dfloat> gd(g.begin(), g.end()), dgd(dg.begin(), dg.end());
+      CK(cudaMemcpy(const_cast<void *>(ap.gain), gd.data(), 8 * ap.n, cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(dptr, dgd.data(), 8 * ap.n, cudaMemcpyHostToDevice));
     } else {
       CK(cudaMemcpy(const_cast<void *>(ap.gain), g.data(), 8 * ap.n, cudaMemcpyHostToDevice));
       CK(cudaMemcpy(dptr, dg.data(), 8 * ap.n, cudaMemcpyHostToDevice));
@@ -125,10 +130,15 @@ int launch_set(scft_ctx *ctx, const AxisPlan &ap, const scft::PassSet<R> &ps, cu
     CKL(scft::launch_fast_line(ap, ps, st));
     return SCFT_OK;
   }
+  if constexpr (std::is_same<R, scft::dfloat>::value) {
+    // scft_create admits double-float contexts only when every pass is fast
+    return scft_fail(ctx, SCFT_ERR_UNSUPPORTED, "double-float pass without a register kernel");
+  } else {
   for (int k = 0; k < ps.nset; ++k)
     CKL(scft::launch_line_filter<R>(ap, ps.in[k], ps.in_bs[k], ps.out[k], ps.out_bs[k],
                                     ps.pre[k], ps.post[k], ps.w_bs, ps.batch, st));
   return SCFT_OK;
+  }
 }
 
 // A march segment: propagator qi over ns steps in field wf, direction sign,
@@ -301,8 +311,9 @@ int run_chain_fused_axes(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t 
 
 int run_chain_fused(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t st, int cidx) {
   if (!ctx->fuse_xy)
-    return ctx->rbytes == 4 ? run_chain_fused_axes<float>(ctx, segs, nseg, st, cidx)
-                            : run_chain_fused_axes<double>(ctx, segs, nseg, st, cidx);
+    return with_real(ctx, [&](auto r) {
+      return run_chain_fused_axes<decltype(r)>(ctx, segs, nseg, st, cidx);
+    });
   const long long M = ctx->M;
   float *tmp[2] = {static_cast<float *>(ctx->tmp[2 * cidx]),
                    static_cast<float *>(ctx->tmp[2 * cidx + 1])};
@@ -367,20 +378,20 @@ int run_chains_any(scft_ctx *ctx, const Seg *const *chains, const int *nseg, int
                    cudaStream_t st, int chain_base = 0) {
   if (nchain == 1 && fused_possible(ctx))
     return run_chain_fused(ctx, chains[0], nseg[0], st, chain_base);
-  return ctx->rbytes == 4 ? run_chains<float>(ctx, chains, nseg, nchain, st, chain_base)
-                          : run_chains<double>(ctx, chains, nseg, nchain, st, chain_base);
+  return with_real(ctx, [&](auto r) {
+    return run_chains<decltype(r)>(ctx, chains, nseg, nchain, st, chain_base);
+  });
 }
 
 // initilize_wdz (cuda_scft.cu:450) for field f into W[f].
 int boltzmann(scft_ctx *ctx, int f, cudaStream_t st) {
   const double *w = f == SCFT_FIELD_WA ? ctx->wa : ctx->wb;
-  if (ctx->rbytes == 4)
-    CKL(scft::launch_boltzmann<float>(w, static_cast<float *>(ctx->W[f]), ctx->M * ctx->batch,
-                                      ctx->p.ds0 / 2, st));
-  else
-    CKL(scft::launch_boltzmann<double>(w, static_cast<double *>(ctx->W[f]), ctx->M * ctx->batch,
-                                       ctx->p.ds0 / 2, st));
-  return SCFT_OK;
+  return with_real(ctx, [&](auto r) {
+    using R = decltype(r);
+    CKL(scft::launch_boltzmann<R>(w, static_cast<R *>(ctx->W[f]), ctx->M * ctx->batch,
+                                  ctx->p.ds0 / 2, st));
+    return SCFT_OK;
+  });
 }
 
 // The march phase of getConc (cuda_scft.cu:77-112) as two lockstep chains:
@@ -483,23 +494,18 @@ int average(scft_ctx *ctx, double *data) {
 
 int set_qint(scft_ctx *ctx, int qi, int s) {
   const long long M = ctx->M;
-  if (qi < 0) {
-    if (ctx->rbytes == 4)
-      CKL(scft::launch_fill<float>(static_cast<float *>(ctx->qint), M, 1.0f, M, ctx->batch, ctx->st));
-    else
-      CKL(scft::launch_fill<double>(static_cast<double *>(ctx->qint), M, 1.0, M, ctx->batch, ctx->st));
+  return with_real(ctx, [&](auto r) {
+    using R = decltype(r);
+    if (qi < 0) {
+      CKL(scft::launch_fill<R>(static_cast<R *>(ctx->qint), M, R(1.0f), M, ctx->batch, ctx->st));
+      return SCFT_OK;
+    }
+    const long long qbs = (long long)(ctx->q_ns[qi] + 1) * M;
+    CKL(scft::launch_copy_slice<R>(static_cast<R *>(ctx->qint), M,
+                                   static_cast<R *>(ctx->q[qi]) + (long long)s * M, qbs, M,
+                                   ctx->batch, ctx->st));
     return SCFT_OK;
-  }
-  const long long qbs = (long long)(ctx->q_ns[qi] + 1) * M;
-  if (ctx->rbytes == 4)
-    CKL(scft::launch_copy_slice<float>(static_cast<float *>(ctx->qint), M,
-                                       static_cast<float *>(ctx->q[qi]) + (long long)s * M, qbs,
-                                       M, ctx->batch, ctx->st));
-  else
-    CKL(scft::launch_copy_slice<double>(static_cast<double *>(ctx->qint), M,
-                                        static_cast<double *>(ctx->q[qi]) + (long long)s * M, qbs,
-                                        M, ctx->batch, ctx->st));
-  return SCFT_OK;
+  });
 }
 
 template <typename R>
@@ -536,7 +542,7 @@ int get_conc(scft_ctx *ctx) {
   if ((rc = prof_begin(ctx))) return rc;
   if ((rc = march_phase_graph(ctx))) return rc;                                // :77-112
   if ((rc = prof_end(ctx, 2.0 * (ctx->NsA + ctx->dNsB) * ctx->M * ctx->batch))) return rc;
-  rc = ctx->rbytes == 4 ? q_and_phi<float>(ctx) : q_and_phi<double>(ctx);
+  rc = with_real(ctx, [&](auto r) { return q_and_phi<decltype(r)>(ctx); });
   ctx->have_conc = rc == SCFT_OK;
   return rc;
 }
@@ -772,6 +778,8 @@ int filter_impl(scft_ctx *ctx, const R *in, long long in_bs, R *out, long long o
 int scft_internal_filter(scft_ctx *ctx, const void *in, long long in_bs, void *out,
                          long long out_bs, const void *pre, const void *post, long long w_bs,
                          int nb, int deriv_pass, void *s0, void *s1, cudaStream_t st) {
+  if (ctx->rkind == kRealDF)
+    return scft_fail(ctx, SCFT_ERR_UNSUPPORTED, "no adjoint or stress for double-float contexts");
   if (ctx->rbytes == 4)
     return filter_impl<float>(ctx, (const float *)in, in_bs, (float *)out, out_bs,
                               (const float *)pre, (const float *)post, w_bs, nb, deriv_pass,
@@ -844,7 +852,8 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad flags");
   if (!(p.lx > 0 && p.ly > 0 && p.lz > 0 && p.ds0 > 0 && p.fA >= 0 && p.fA <= 1 && p.batch >= 1))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
-  if (p.precision != SCFT_PREC_FP64 && p.precision != SCFT_PREC_FP32)
+  if (p.precision != SCFT_PREC_FP64 && p.precision != SCFT_PREC_FP32 &&
+      p.precision != SCFT_PREC_DF)
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad precision");
   if (p.mixing < SCFT_MIX_SIMPLE || p.mixing > SCFT_MIX_CONSTRAINED_EX)
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad mixing mode");
@@ -869,6 +878,8 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
   ctx->M = (long long)p.nx * p.ny * p.nz;
   ctx->batch = p.batch;
   ctx->rbytes = p.precision == SCFT_PREC_FP32 ? 4 : 8;
+  ctx->rkind = p.precision == SCFT_PREC_FP32 ? kRealF32
+               : p.precision == SCFT_PREC_DF ? kRealDF : kRealF64;
   ctx->NsA = (int)(p.fA / p.ds0 + 1.0e-8);            // init_cuda.cu:330
   ctx->dNsB = (int)((1 - p.fA) / p.ds0 + 1.0e-8);     // init_cuda.cu:329,331
   ctx->q_ns[SCFT_Q_A] = ctx->q_ns[SCFT_Q_CA] = ctx->NsA;
@@ -968,6 +979,10 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     if (tl > n_pairs) tl = n_pairs;
     ap.tl = tl;
     ap.use_fast = scft::fast_line_supported(ap, rb) ? 1 : 0;
+    if (ctx->rkind == kRealDF && !ap.use_fast)
+      return fail(SCFT_ERR_UNSUPPORTED,
+                  "double-float propagation needs register-resident passes: Nx of 64 or "
+                  "128, Ny and Nz of 1, 32, 64 or 128, Ny*Nz a multiple of 64");
     if (scft::line_filter_smem_bytes(ap, rb) > (size_t)scft::kLineSmemMax)
       return fail(SCFT_ERR_UNSUPPORTED, "line too long for shared memory");
     // twiddles exp(-2 pi i m / n); the gains are filled by upload_gains
@@ -978,6 +993,9 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
       if (rb == 4) {
         float *t = reinterpret_cast<float *>(&host[tw_off]);
         t[2 * m] = (float)c; t[2 * m + 1] = (float)s;
+      } else if (ctx->rkind == kRealDF) {
+        scft::dfloat *t = reinterpret_cast<scft::dfloat *>(&host[tw_off]);
+        t[2 * m] = scft::dfloat(c); t[2 * m + 1] = scft::dfloat(s);
       } else {
         double *t = reinterpret_cast<double *>(&host[tw_off]);
         t[2 * m] = c; t[2 * m + 1] = s;
@@ -1090,12 +1108,13 @@ int scft_get_q(scft_ctx *ctx, int q, int s, double *dst) {
   // stage through the (FP64-sized) phi scratch: cast on the device, then copy
   double *stage = nullptr;
   CK(cudaMallocAsync((void **)&stage, sizeof(double) * M * ctx->batch, ctx->st));
-  if (ctx->rbytes == 4)
-    CKL(scft::launch_cast_slice<float>(stage, M, static_cast<float *>(ctx->q[q]) + (long long)s * M,
-                                       qbs, M, ctx->batch, ctx->st));
-  else
-    CKL(scft::launch_cast_slice<double>(stage, M, static_cast<double *>(ctx->q[q]) + (long long)s * M,
-                                        qbs, M, ctx->batch, ctx->st));
+  int rc = with_real(ctx, [&](auto r) {
+    using R = decltype(r);
+    CKL(scft::launch_cast_slice<R>(stage, M, static_cast<R *>(ctx->q[q]) + (long long)s * M, qbs,
+                                   M, ctx->batch, ctx->st));
+    return SCFT_OK;
+  });
+  if (rc) return rc;
   CK(cudaMemcpyAsync(dst, stage, sizeof(double) * M * ctx->batch, cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaFreeAsync(stage, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
@@ -1239,14 +1258,13 @@ int scft_copy_q_reference_layout(scft_ctx *ctx, int q, double *dst_device) {
   if (!ctx || !dst_device || q < 0 || q > 3)
     return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad propagator or null pointer");
   CK(cudaSetDevice(ctx->p.device));
-  if (ctx->rbytes == 4)
-    CKL(scft::launch_q_to_reference_layout<float>(static_cast<const float *>(ctx->q[q]),
-                                                  ctx->q_ns[q], ctx->M, ctx->batch, dst_device,
-                                                  ctx->st));
-  else
-    CKL(scft::launch_q_to_reference_layout<double>(static_cast<const double *>(ctx->q[q]),
-                                                   ctx->q_ns[q], ctx->M, ctx->batch, dst_device,
-                                                   ctx->st));
+  int rc = with_real(ctx, [&](auto r) {
+    using R = decltype(r);
+    CKL(scft::launch_q_to_reference_layout<R>(static_cast<const R *>(ctx->q[q]), ctx->q_ns[q],
+                                              ctx->M, ctx->batch, dst_device, ctx->st));
+    return SCFT_OK;
+  });
+  if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->st));
   return SCFT_OK;
 }

@@ -4,12 +4,15 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "dfloat.cuh"
+
 namespace scft {
 
 // Complex type matched to the working real type.
 template <typename R> struct cplx;
 template <> struct cplx<float> { typedef float2 type; };
 template <> struct cplx<double> { typedef double2 type; };
+template <> struct cplx<dfloat> { typedef dfloat2 type; };
 
 template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
   C r;

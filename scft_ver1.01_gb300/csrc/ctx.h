@@ -16,6 +16,7 @@ struct scft_ctx {
   long long M = 0;
   int batch = 0;
   int rbytes = 8;               // sizeof working real (4 or 8)
+  int rkind = 1;                // working real: kRealF32, kRealF64 or kRealDF
   cudaStream_t st = nullptr;    // the context's stream (every launch)
   bool use_graph = true;        // march phase replayed as a CUDA graph
   bool capturing = false;       // inside a group graph capture: launch directly
@@ -72,6 +73,15 @@ struct scft_ctx {
   size_t prof_used = 0;
   double prof_point_steps = 0.0;
 };
+
+// The working real type of the propagators (float, double or the
+// double-float pair), and a dispatch on it: with_real(ctx, f) calls f(R{}).
+constexpr int kRealF32 = 0, kRealF64 = 1, kRealDF = 2;
+template <typename F> int with_real(const scft_ctx *ctx, F &&f) {
+  if (ctx->rkind == kRealF32) return f(float{});
+  if (ctx->rkind == kRealDF) return f(scft::dfloat{});
+  return f(double{});
+}
 
 // NVTX range for profilers (a no-op unless a tool is attached).
 struct NvtxRange {

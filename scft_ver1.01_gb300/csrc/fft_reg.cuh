@@ -55,6 +55,7 @@ __host__ __device__ __forceinline__ void static_for(F &&f) {
 template <typename C> struct real_of;
 template <> struct real_of<float2> { typedef float type; };
 template <> struct real_of<double2> { typedef double type; };
+template <> struct real_of<dfloat2> { typedef dfloat type; };
 
 // v * exp(-/+ 2 pi i m / R), exact for multiples of a quarter turn.
 template <int M, int R, bool INV, typename C>

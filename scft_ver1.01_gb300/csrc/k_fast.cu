@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
   C *s_tw = reinterpret_cast<C *>(smem_raw + fast_core_smem<T, N, XP>());
   T *s_g = reinterpret_cast<T *>(s_tw + N);
   for (int i = threadIdx.x; i < N; i += NT) {
-    s_tw[i] = __ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
-    s_g[i] = __ldg(reinterpret_cast<const T *>(ap.gain) + i);
+    s_tw[i] = ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
+    s_g[i] = ldg(reinterpret_cast<const T *>(ap.gain) + i);
   }
   // Column passes with a post factor: the factor's tile does not depend on
   // the previous pass either, so its cp.async copies are issued here too and
@@ -159,8 +159,8 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
 #pragma unroll
     for (int i = threadIdx.x; i < 64 * N; i += NT) {
       const int r = i / N, c = i % N;
-      T x = __ldg(src + i);
-      if (wsrc) x *= __ldg(wsrc + i);
+      T x = ldg(src + i);
+      if (wsrc) x *= ldg(wsrc + i);
       stg[r * PITCH + c] = x;
     }
     __syncthreads();
@@ -175,13 +175,13 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
     const T *src = in + b * in_bs + base;
     reg::static_for<0, R1>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
-      v[j] = __ldg(reinterpret_cast<const C *>(src + (long long)(p + P * j) * ap.s_n));
+      v[j] = ldg(reinterpret_cast<const C *>(src + (long long)(p + P * j) * ap.s_n));
     });
     if (pre) {
       const T *ws = pre + b * w_bs + base;
       reg::static_for<0, R1>([&](auto j_) {
         constexpr int j = decltype(j_)::value;
-        const C w = __ldg(reinterpret_cast<const C *>(ws + (long long)(p + P * j) * ap.s_n));
+        const C w = ldg(reinterpret_cast<const C *>(ws + (long long)(p + P * j) * ap.s_n));
         v[j].x *= w.x;
         v[j].y *= w.y;
       });
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
     for (int i = threadIdx.x; i < 64 * N; i += NT) {
       const int r = i / N, c = i % N;
       T x = stg[r * PITCH + c];
-      if (wdst) x *= __ldg(wdst + i);
+      if (wdst) x *= ldg(wdst + i);
       dst[i] = x;
     }
   } else {
@@ -531,8 +531,8 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<T> ps) {
   C *s_tw = reinterpret_cast<C *>(smem_raw + fast_core_smem<T, N, false>());
   T *s_g = reinterpret_cast<T *>(s_tw + N);
   for (int i = threadIdx.x; i < N; i += NT) {
-    s_tw[i] = __ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
-    s_g[i] = __ldg(reinterpret_cast<const T *>(ap.gain) + i);
+    s_tw[i] = ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
+    s_g[i] = ldg(reinterpret_cast<const T *>(ap.gain) + i);
   }
   T *s_wt = reinterpret_cast<T *>(smem_raw + fast_wtile_off<T, N, false>());
   const long long tile = (long long)blockIdx.y * ap.s_outer + (long long)blockIdx.x * 64;
@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<T> ps) {
     const T *src = in + b * ps.in_bs[set] + base;
     reg::static_for<0, R1>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
-      v[j] = __ldg(reinterpret_cast<const C *>(src + (long long)(p + P * j) * ap.s_n));
+      v[j] = ldg(reinterpret_cast<const C *>(src + (long long)(p + P * j) * ap.s_n));
     });
   }
   __syncthreads();   // the shared tables are complete
@@ -609,8 +609,8 @@ __global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<T> ps) {
   C *s_tw = reinterpret_cast<C *>(smem_raw + fast_core_smem<T, N, true>());
   T *s_g = reinterpret_cast<T *>(s_tw + N);
   for (int i = threadIdx.x; i < N; i += NT) {
-    s_tw[i] = __ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
-    s_g[i] = __ldg(reinterpret_cast<const T *>(ap.gain) + i);
+    s_tw[i] = ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
+    s_g[i] = ldg(reinterpret_cast<const T *>(ap.gain) + i);
   }
   const long long base = (long long)blockIdx.x * 64 * N;   // 64 consecutive rows
   T *s_wt = reinterpret_cast<T *>(smem_raw + xx_wtile_off<T, N>());
@@ -627,7 +627,7 @@ __global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<T> ps) {
   pdl_release();
   const T *src = ps.in[set] + b * ps.in_bs[set] + base;
 #pragma unroll
-  for (int i = threadIdx.x; i < 64 * N; i += NT) stg[(i / N) * PITCH + (i % N)] = __ldg(src + i);
+  for (int i = threadIdx.x; i < 64 * N; i += NT) stg[(i / N) * PITCH + (i % N)] = ldg(src + i);
   __syncthreads();
   C v[R1];
   auto rows_to_regs = [&]() {
@@ -917,15 +917,56 @@ cudaError_t launch_xx(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t
     default: return cudaErrorInvalidValue;
   }
 }
-cudaError_t launch_xx(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st) {
+// 8-byte reals (FP64 and double-float): lines up to 128 points fit the registers
+namespace {
+template <typename T>
+cudaError_t launch_xx_wide(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
   if (ps.nset < 1 || ps.nset > kMaxSet || !ap.n_fast) return cudaErrorInvalidValue;
   if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
   switch (ap.n) {
-    case 32: return launch_xx_t<double, 32, 4>(ap, ps, st);
-    case 64: return launch_xx_t<double, 64, 8>(ap, ps, st);
-    case 128: return launch_xx_t<double, 128, 8>(ap, ps, st);
+    case 32: return launch_xx_t<T, 32, 4>(ap, ps, st);
+    case 64: return launch_xx_t<T, 64, 8>(ap, ps, st);
+    case 128: return launch_xx_t<T, 128, 8>(ap, ps, st);
     default: return cudaErrorInvalidValue;
   }
+}
+template <typename T>
+cudaError_t launch_zz_wide(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
+  if (ps.nset < 1 || ps.nset > kMaxSet || ap.n_fast) return cudaErrorInvalidValue;
+  if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
+  switch (ap.n) {
+    case 32: return launch_zz_t<T, 32, 4>(ap, ps, st);
+    case 64: return launch_zz_t<T, 64, 8>(ap, ps, st);
+    case 128: return launch_zz_t<T, 128, 8>(ap, ps, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+template <typename T>
+cudaError_t launch_fast_line_wide(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
+  if (ps.nset < 1 || ps.nset > kMaxSet) return cudaErrorInvalidValue;
+  for (int k = 0; k < ps.nset; ++k)
+    if ((reinterpret_cast<uintptr_t>(ps.post[k]) | reinterpret_cast<uintptr_t>(ps.pre[k]) |
+         reinterpret_cast<uintptr_t>(ps.in[k]) | reinterpret_cast<uintptr_t>(ps.out[k])) & 15)
+      return cudaErrorMisalignedAddress;
+  const bool xp = ap.n_fast != 0;
+  switch (ap.n) {
+    case 32:
+      return xp ? launch_one<T, 32, 4, true>(ap, ps, st) : launch_one<T, 32, 4, false>(ap, ps, st);
+    case 64:
+      return xp ? launch_one<T, 64, 8, true>(ap, ps, st) : launch_one<T, 64, 8, false>(ap, ps, st);
+    case 128:
+      return xp ? launch_one<T, 128, 8, true>(ap, ps, st)
+                : launch_one<T, 128, 8, false>(ap, ps, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+}  // namespace
+
+cudaError_t launch_xx(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st) {
+  return launch_xx_wide(ap, ps, st);
+}
+cudaError_t launch_xx(const AxisPlan &ap, const PassSet<dfloat> &ps, cudaStream_t st) {
+  return launch_xx_wide(ap, ps, st);
 }
 
 cudaError_t launch_wait_selftest(unsigned *err, long long limit, cudaStream_t st) {
@@ -945,14 +986,10 @@ cudaError_t launch_zz(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t
   }
 }
 cudaError_t launch_zz(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st) {
-  if (ps.nset < 1 || ps.nset > kMaxSet || ap.n_fast) return cudaErrorInvalidValue;
-  if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
-  switch (ap.n) {
-    case 32: return launch_zz_t<double, 32, 4>(ap, ps, st);
-    case 64: return launch_zz_t<double, 64, 8>(ap, ps, st);
-    case 128: return launch_zz_t<double, 128, 8>(ap, ps, st);
-    default: return cudaErrorInvalidValue;
-  }
+  return launch_zz_wide(ap, ps, st);
+}
+cudaError_t launch_zz(const AxisPlan &ap, const PassSet<dfloat> &ps, cudaStream_t st) {
+  return launch_zz_wide(ap, ps, st);
 }
 
 cudaError_t launch_xyxy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
@@ -993,6 +1030,9 @@ cudaError_t fast_line_prepare() {
   PREP(double, 32, 4)
   PREP(double, 64, 8)
   PREP(double, 128, 8)
+  PREP(dfloat, 32, 4)
+  PREP(dfloat, 64, 8)
+  PREP(dfloat, 128, 8)
 #undef PREP
   int dev = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
@@ -1019,6 +1059,9 @@ cudaError_t fast_line_prepare() {
   PREP_FUSED(double, 32, 4)
   PREP_FUSED(double, 64, 8)
   PREP_FUSED(double, 128, 8)
+  PREP_FUSED(dfloat, 32, 4)
+  PREP_FUSED(dfloat, 64, 8)
+  PREP_FUSED(dfloat, 128, 8)
 #undef PREP_FUSED
   return e;
 }
@@ -1061,24 +1104,10 @@ cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaS
 }
 
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st) {
-  if (ps.nset < 1 || ps.nset > kMaxSet) return cudaErrorInvalidValue;
-  for (int k = 0; k < ps.nset; ++k)
-    if ((reinterpret_cast<uintptr_t>(ps.post[k]) | reinterpret_cast<uintptr_t>(ps.pre[k]) |
-         reinterpret_cast<uintptr_t>(ps.in[k]) | reinterpret_cast<uintptr_t>(ps.out[k])) & 15)
-      return cudaErrorMisalignedAddress;
-  const bool xp = ap.n_fast != 0;
-  switch (ap.n) {
-    case 32:
-      return xp ? launch_one<double, 32, 4, true>(ap, ps, st)
-                : launch_one<double, 32, 4, false>(ap, ps, st);
-    case 64:
-      return xp ? launch_one<double, 64, 8, true>(ap, ps, st)
-                : launch_one<double, 64, 8, false>(ap, ps, st);
-    case 128:
-      return xp ? launch_one<double, 128, 8, true>(ap, ps, st)
-                : launch_one<double, 128, 8, false>(ap, ps, st);
-    default: return cudaErrorInvalidValue;
-  }
+  return launch_fast_line_wide(ap, ps, st);
+}
+cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<dfloat> &ps, cudaStream_t st) {
+  return launch_fast_line_wide(ap, ps, st);
 }
 
 }  // namespace scft

@@ -198,6 +198,32 @@ __global__ void k_contour_phi<float>(const float *__restrict__ q, const float *_
   }
 }
 
+// Double-float propagators: products and sums in pair arithmetic (FP32 pipe),
+// one conversion to FP64 per point.
+template <>
+__global__ void k_contour_phi<dfloat>(const dfloat *__restrict__ q, const dfloat *__restrict__ qc,
+                                      int ns, long long M, const double *__restrict__ ffl,
+                                      double *__restrict__ phi, ContourWeights cw) {
+  const int b = blockIdx.y;
+  const long long qbs = (long long)(ns + 1) * M;
+  const dfloat *qb = q + b * qbs, *qcb = qc + b * qbs;
+  const bool trap = cw.c_odd == 1.0 && cw.c_even == 1.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x) {
+    dfloat ao, ae;
+    for (int s = 1; s < cw.m; ++s) {
+      const dfloat pr = qb[s * M + i] * qcb[s * M + i];
+      if (trap || (s & 1)) ao += pr;
+      else ae += pr;
+    }
+    double ends = 0.0;
+    for (int k = 0; k < cw.nspec; ++k)
+      ends += cw.w[k] * ((double)qb[cw.s[k] * M + i] * (double)qcb[cw.s[k] * M + i]);
+    const double inner = trap ? (double)ao : cw.c_odd * (double)ao + cw.c_even * (double)ae;
+    phi[b * M + i] = (inner + ends) * ffl[b];
+  }
+}
+
 __global__ void k_phi_w(double *__restrict__ wa, double *__restrict__ wb,
                         const double *__restrict__ pha, const double *__restrict__ phb,
                         double hAB, double wopt, double wcmp, long long n) {
@@ -469,6 +495,8 @@ template cudaError_t launch_q_to_reference_layout<float>(const float *, int, lon
                                                          double *, cudaStream_t);
 template cudaError_t launch_q_to_reference_layout<double>(const double *, int, long long, int,
                                                           double *, cudaStream_t);
+template cudaError_t launch_q_to_reference_layout<dfloat>(const dfloat *, int, long long, int,
+                                                          double *, cudaStream_t);
 
 cudaError_t launch_phi_w_constrained(double *wa, double *wb, const double *pha, const double *phb,
                                      const double *target, double hAB, double lambda, int ex,
@@ -507,6 +535,7 @@ cudaError_t launch_free_energy_finalize(const double *partial, int nblk, int bat
                                              const double *, double *, bool, cudaStream_t);
 INST(float)
 INST(double)
+INST(dfloat)
 #undef INST
 
 }  // namespace scft

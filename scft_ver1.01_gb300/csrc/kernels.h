@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "dfloat.cuh"
+
 namespace scft {
 
 // One per-axis pass of the separable diffusion operator exp(-k^2 ds):
@@ -59,6 +61,7 @@ cudaError_t fast_line_prepare();
 cudaError_t launch_wait_selftest(unsigned *err, long long limit, cudaStream_t st);
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st);
+cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<dfloat> &ps, cudaStream_t st);
 // Fused step pairs.  The axis filters commute, so consecutive contour steps
 // can run their passes in alternating order (x+y then z, z then x+y); the
 // end of one step and the start of the next are then the same pass type and
@@ -66,9 +69,11 @@ cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<double> &ps, cuda
 // K_a the z filter (launch_zz) or the x+y filters (launch_xyxy).
 cudaError_t launch_zz(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
 cudaError_t launch_zz(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st);
+cudaError_t launch_zz(const AxisPlan &ap, const PassSet<dfloat> &ps, cudaStream_t st);
 // the same on x lines (rows contiguous), for grids without the x+y plane
 cudaError_t launch_xx(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);
 cudaError_t launch_xx(const AxisPlan &ap, const PassSet<double> &ps, cudaStream_t st);
+cudaError_t launch_xx(const AxisPlan &ap, const PassSet<dfloat> &ps, cudaStream_t st);
 cudaError_t launch_xyxy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
                         cudaStream_t st);
 

@@ -121,6 +121,76 @@ def test_simpson_uniform_field_gives_the_block_fractions(pkg):
             np.testing.assert_allclose(ctx.phb, 0.65, rtol=1e-13)
 
 
+# register-resident passes on every axis: Nx in {64, 128}, Ny and Nz in
+# {1, 32, 64, 128}, Ny*Nz a multiple of 64
+DF_GRIDS = [GRIDS[7], GRIDS[8], GRIDS[9], (64, 64, 64, 3.8, 3.8, 3.8), (128, 32, 64, 5.0, 3.0, 4.0)]
+
+
+@pytest.mark.parametrize("g", DF_GRIDS)
+def test_double_float_parity(pkg, orc, g):
+    """SCFT_PREC_DF: propagation in FP32-pair arithmetic must reach FP64-level
+    agreement with the FP64 oracle (the FP32 path stops near 1e-6)."""
+    from scft_gb300 import fields
+    kw = dict(hAB=18.0, fA=0.36, ds0=0.01)
+    p = oparams(orc, g, **kw)
+    wa, wb = fields.gyroid(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 18.0, seed=4, batch=2)
+    ref = orc.get_conc(wa, wb, p)
+    with make_ctx(pkg, g, pkg.PREC_DF, **kw) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.get_conc()
+        assert rel(ctx.pha, ref.pha) < 1e-10
+        assert rel(ctx.phb, ref.phb) < 1e-10
+        assert np.abs(ctx.Q() / ref.Q - 1).max() < 1e-10
+        assert rel(ctx.get_q(pkg.Q_A, p.NsA), ref.qa[:, p.NsA]) < 1e-10
+        assert rel(ctx.get_q(pkg.Q_CB, 0), ref.qcb[:, 0]) < 1e-10
+
+
+def test_double_float_limits(pkg):
+    """Grids without register-resident passes on every axis, and the adjoint
+    and the stress, are refused (status, no fallback)."""
+    for n in ((48, 48, 48), (32, 32, 32), (256, 64, 64)):
+        with pytest.raises(pkg.ScftError) as e:
+            pkg.Context(nx=n[0], ny=n[1], nz=n[2], precision=pkg.PREC_DF)
+        assert e.value.status == pkg.ERR_UNSUPPORTED
+    with pkg.Context(nx=64, ny=32, nz=32, precision=pkg.PREC_DF) as ctx:
+        z = np.zeros(ctx.shape)
+        ctx.set_w(z, z)
+        ctx.get_conc()
+        np.testing.assert_allclose(ctx.pha, 0.5, rtol=1e-13)
+        with pytest.raises(pkg.ScftError) as e:
+            ctx.stress()
+        assert e.value.status == pkg.ERR_UNSUPPORTED
+        with pytest.raises(pkg.ScftError) as e:
+            ctx.adjoint(z, z, np.zeros(1))
+        assert e.value.status == pkg.ERR_UNSUPPORTED
+
+
+def test_double_float_polish_matches_fp64(pkg):
+    """FP32 solve, then the double-float polish: the same saddle point as the
+    plain FP64 path (F, Q and phi at FP64 level once both reach 1e-8)."""
+    from scft_gb300 import fields
+    g = dict(nx=64, ny=32, nz=32, lx=3.8, ly=3.8, lz=3.8, hAB=18.0, fA=0.36, ds0=0.01,
+             mixing=pkg.MIX_ANDERSON, anderson_history=20, anderson_start=1e9)
+    wa, wb = fields.gyroid(64, 32, 32, 3.8, 3.8, 3.8, 18.0, seed=0)
+    with pkg.Context(precision=pkg.PREC_FP64, **g) as c64:
+        c64.set_w(wa, wb)
+        _, fe64 = c64.converge(1e-8, 2000)
+        pha64, Q64 = c64.pha, c64.Q()
+    with pkg.Context(precision=pkg.PREC_FP32, **g) as c32, \
+            pkg.Context(precision=pkg.PREC_DF, **g) as cdf:
+        c32.set_w(wa, wb)
+        c32.converge(3e-5, 2000)
+        cdf.copy_fields_from(c32)
+        it, fedf = cdf.converge(1e-8, 2000)
+        assert cdf.residual()[0][0] < 1e-8
+        phadf, Qdf = cdf.pha, cdf.Q()
+    assert abs(fedf[0, 0] - fe64[0, 0]) < 1e-9
+    assert abs(Qdf[0] / Q64[0] - 1) < 1e-8
+    # up to the translational zero mode of the converged structure
+    spec = lambda a: np.abs(np.fft.rfftn(a[0]))
+    assert np.abs(spec(phadf) - spec(pha64)).max() < 1e-6 * spec(pha64).max()
+
+
 def test_average_value_and_phi_w(pkg, orc):
     g = GRIDS[1]
     p = oparams(orc, g, hAB=15.0)
