@@ -96,7 +96,10 @@ int init_scft(CUFFT_INFO *cufft_info, GPU_INFO *gpu_info, int argc, char **argv)
     printf("It could as well be set by adding flag -step=Num. \n");
   }
   const char *prec = flag_value(argc, argv, "precision");
-  cufft_info->precision = (prec && !strcasecmp(prec, "fp32")) ? SCFT_PREC_FP32 : SCFT_PREC_FP64;
+  cufft_info->precision = !prec                      ? SCFT_PREC_FP64
+                          : !strcasecmp(prec, "fp32") ? SCFT_PREC_FP32
+                          : !strcasecmp(prec, "df")   ? SCFT_PREC_DF
+                                                      : SCFT_PREC_FP64;
   const char *metrics = flag_value(argc, argv, "metrics");
   snprintf(cufft_info->metrics, sizeof cufft_info->metrics, "%s", metrics ? metrics : "");
   if (type) {

@@ -53,7 +53,8 @@ int scft_read_ab_txt(const char *path, scft_params *p, int *intag) {
       } else if (key == "precision") {
         if (val == "fp32") p->precision = SCFT_PREC_FP32;
         else if (val == "fp64") p->precision = SCFT_PREC_FP64;
-        else err = "precision must be fp32 or fp64";
+        else if (val == "df") p->precision = SCFT_PREC_DF;
+        else err = "precision must be fp32, fp64 or df";
       } else if (!num) {
         err = "not a number";
       } else if (key == "history") {

@@ -104,6 +104,8 @@ def test_read_ab_txt_optional_keys(pkg, tmp_path):
     assert p.mixing == pkg.MIX_ANDERSON and p.anderson_history == 30
     assert (p.anderson_lambda, p.anderson_start, p.wopt, p.wcmp) == (0.4, 0.5, 0.02, 0.2)
     assert p.precision == pkg.PREC_FP32 and p.ds0 == 1.0 / 400
+    f.write_text(AB7 + "precision=df\n")
+    assert pkg.read_ab_txt(str(f))[0].precision == pkg.PREC_DF
     # without the optional lines: the reference's defaults
     f.write_text(AB7)
     p, _ = pkg.read_ab_txt(str(f))
