@@ -11,7 +11,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-G = dict(nx=32, ny=32, nz=16, lx=3.8, ly=3.8, lz=1.9, hAB=18.0, fA=0.36, ds0=0.01)
+# Nx = 64 so that the double-float path (register kernels on every axis) runs too
+G = dict(nx=64, ny=32, nz=32, lx=7.6, ly=3.8, lz=3.8, hAB=18.0, fA=0.36, ds0=0.01)
 
 
 def start_fields(batch=2):
@@ -21,7 +22,8 @@ def start_fields(batch=2):
 
 
 def ctx_kw(pkg, prec, mixing, **extra):
-    kw = dict(G, batch=2, precision=pkg.PREC_FP32 if prec == "fp32" else pkg.PREC_FP64)
+    kw = dict(G, batch=2, precision={"fp32": pkg.PREC_FP32, "df": pkg.PREC_DF}.get(
+        prec, pkg.PREC_FP64))
     if mixing == "anderson":
         kw.update(mixing=pkg.MIX_ANDERSON, anderson_history=5, anderson_start=1e9)
     kw.update(extra)
@@ -29,7 +31,7 @@ def ctx_kw(pkg, prec, mixing, **extra):
 
 
 @pytest.mark.parametrize("mixing", ["simple", "anderson"])
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "df"])
 def test_resume_repeats_the_run_bit_for_bit(pkg, tmp_path, prec, mixing):
     wa, wb = start_fields()
     path = tmp_path / "run.ckpt"
@@ -79,7 +81,7 @@ def test_checkpoint_errors(pkg, tmp_path):
     with pkg.Context(**ctx_kw(pkg, "fp64", "simple")) as a:
         a.set_w(wa, wb)
         a.save_checkpoint(path)
-    with pkg.Context(**dict(ctx_kw(pkg, "fp64", "simple"), nz=8, lz=0.95)) as b:
+    with pkg.Context(**dict(ctx_kw(pkg, "fp64", "simple"), nz=16, lz=1.9)) as b:
         with pytest.raises(pkg.ScftError) as e:
             b.load_checkpoint(path)
         assert e.value.status == pkg.ERR_INVALID_ARG

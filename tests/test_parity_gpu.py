@@ -145,6 +145,22 @@ def test_double_float_parity(pkg, orc, g):
         assert rel(ctx.get_q(pkg.Q_CB, 0), ref.qcb[:, 0]) < 1e-10
 
 
+@pytest.mark.parametrize("g,fA,ds0", [(GRIDS[7], 0.45, 0.01), (GRIDS[8], 0.36, 0.005)])
+def test_double_float_simpson_parity(pkg, orc, g, fA, ds0):
+    """The double-float contour sum with Simpson weights (both weight classes,
+    the closing 3/8 rule for odd blocks)."""
+    from scft_gb300 import fields
+    kw = dict(hAB=20.0, fA=fA, ds0=ds0)
+    p = oparams(orc, g, simpson=True, **kw)
+    wa, wb = fields.lamellar(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 20.0, seed=3, batch=2)
+    ref = orc.get_conc(wa, wb, p)
+    with make_ctx(pkg, g, pkg.PREC_DF, flags=pkg.FLAG_SIMPSON, **kw) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.get_conc()
+        assert rel(ctx.pha, ref.pha) < 1e-10
+        assert rel(ctx.phb, ref.phb) < 1e-10
+
+
 def test_double_float_limits(pkg):
     """Grids without register-resident passes on every axis, and the adjoint
     and the stress, are refused (status, no fallback)."""
