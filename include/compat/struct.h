@@ -8,7 +8,8 @@
  *   - the *_cu vectors hold one device pointer each (index 0);
  *   - wa_cu/wb_cu/pha_cu/phb_cu are FP64 [batch][Nz][Ny][Nx] device arrays;
  *   - qa_cu/qb_cu/qca_cu/qcb_cu point at contour-outer propagator storage
- *     ([batch][s][Nz][Ny][Nx], FP64 or FP32), not the reference's s-fastest
+ *     ([batch][s][Nz][Ny][Nx] in the propagation precision: FP64, FP32, or
+ *     double-float pairs {float hi, lo}), not the reference's s-fastest
  *     g[b][r][s] -- unless the driver is compiled with
  *     -DSCFT_COMPAT_FP64_LAYOUT: then they point at FP64 mirrors in the
  *     reference's layout, refreshed by getConc and sovDifFft;
@@ -85,7 +86,7 @@ typedef struct {
   std::vector<double *> qcb_cu;
   /* GB300 build: the context behind the fields above */
   scft_ctx *gb300;
-  int precision;     /* SCFT_PREC_FP64 (default) or SCFT_PREC_FP32 */
+  int precision;     /* SCFT_PREC_FP64 (default), SCFT_PREC_FP32 or SCFT_PREC_DF */
   /* 1: qa_cu/qb_cu/qca_cu/qcb_cu are FP64 mirrors in the reference's
    * g[b][r][s] layout (set by -DSCFT_COMPAT_FP64_LAYOUT in the driver) */
   int reference_layout = SCFT_COMPAT_REFERENCE_LAYOUT;
