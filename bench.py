@@ -296,6 +296,7 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
         # polish at 3e-5 (measured: 48 FP64 polish iterations, against 76 from 1e-4)
         it32, _, _ = converge_timed(c32, 3e-5, max_it, budget_s)
         t32 = time.perf_counter() - t0
+        w32 = (c32.wa, c32.wb)
         for name, pol, key in (("fp32_fp64_polish", p64, "fp64"), ("fp32_df_polish", pdf, "df")):
             t1 = time.perf_counter()
             pol.copy_fields_from(c32)
@@ -310,6 +311,20 @@ def converge_leg(pkg, dev, tol=1e-6, max_it=3000, budget_s=150.0):
             if ok and ref_t is not None:
                 res["at_tol_1e-7"] = compare_to_fp64(ref_t, state(pol, fe))
             out[name] = res
+        # errors of the FP32-propagation path against the FP64 path (the CPU
+        # oracle's discretisation, matched to 1e-11) at the same fields: the
+        # FP32 solve's end point
+        ev = {}
+        for c in (c32, p64):
+            c.set_w(*w32)
+            c.get_conc()
+            ev[c] = (c.pha, c.phb, c.Q(), c.free_energy()[0])
+        a, b = ev[c32], ev[p64]
+        out["fp32_errors_vs_fp64_same_fields"] = {
+            "phiA_rel": float(np.abs(a[0] - b[0]).max() / np.abs(b[0]).max()),
+            "phiB_rel": float(np.abs(a[1] - b[1]).max() / np.abs(b[1]).max()),
+            "Q_rel": float(abs(a[2][0] / b[2][0] - 1)),
+            "F_abs": float(abs(a[3][0] - b[3][0])), "F_rel": float(abs(a[3][0] / b[3][0] - 1))}
     # the headline: the faster polish that meets the F criterion (1e-7)
     ok = [k for k in ("fp32_df_polish", "fp32_fp64_polish")
           if out[k]["converged"] and out[k]["F_abs_diff"] < 1e-7]

@@ -15,6 +15,8 @@
 // memory (row pitch N+1 floats, conflict-free) and packs rows (l, l+32).
 // The Boltzmann factor of the split step is applied on load (pre) and on
 // store (post), so q makes one round trip per pass.
+#include <type_traits>
+
 #include "common.cuh"
 #include "fft_reg.cuh"
 #include "kernels.h"
@@ -85,6 +87,73 @@ __device__ __forceinline__ void four_step(C (&v)[N / P], C *ex, const C *tw, con
   reg::dft<R1, true>(v);
   group_sync(bar_id, P * 32);   // the exchange buffer is free again
 }
+
+template <int R, typename C> __device__ __forceinline__ void conj_all(C (&a)[R]) {
+#pragma unroll
+  for (int i = 0; i < R; ++i) a[i].y = -a[i].y;
+}
+
+// The same filter with less code, for the double-float type: each pair
+// operation is 7-11 FP32 instructions, and the fully unrolled four_step (four
+// codelets, called twice per fused kernel) overflows the instruction cache
+// (measured: instruction-fetch stalls dominate).  Here the inverse DFTs are
+// conj(DFT(conj(x))) and the forward and inverse halves run as rolled loops,
+// so each codelet is emitted once.  Synchronises the whole CTA (bar 0).
+template <int N, int P, typename C, typename T>
+__device__ __forceinline__ void four_step_compact(C (&v)[N / P], C *ex, const C *tw,
+                                                  const T *gain, int p, int lane) {
+  constexpr int R1 = N / P;
+#pragma unroll 1
+  for (int phase = 0; phase < 2; ++phase) {
+    if (phase == 1) {
+      reg::static_for<0, R1>([&](auto k_) {
+        constexpr int k1 = decltype(k_)::value;
+        v[k1] = ex[(k1 * P + p) * 32 + lane];
+      });
+      conj_all(v);
+    }
+    reg::dft<R1, false>(v);
+    if (phase == 1) {
+      conj_all(v);
+      break;
+    }
+    reg::static_for<0, R1>([&](auto k_) {
+      constexpr int k1 = decltype(k_)::value;
+      if (k1 > 0) v[k1] = cmul(v[k1], tw[p * k1]);
+      ex[(k1 * P + p) * 32 + lane] = v[k1];
+    });
+    __syncthreads();
+    for (int k1 = p; k1 < R1; k1 += P) {
+      C u[P];
+      reg::static_for<0, P>([&](auto q_) {
+        constexpr int q = decltype(q_)::value;
+        u[q] = ex[(k1 * P + q) * 32 + lane];
+      });
+#pragma unroll 1
+      for (int dir = 0; dir < 2; ++dir) {
+        reg::dft<P, false>(u);
+        if (dir == 1) break;
+        reg::static_for<0, P>([&](auto k2_) {
+          constexpr int k2 = decltype(k2_)::value;
+          const T g = gain[k1 + R1 * k2];
+          u[k2].x *= g;
+          u[k2].y *= g;
+        });
+        conj_all(u);
+      }
+      conj_all(u);
+      reg::static_for<0, P>([&](auto q_) {
+        constexpr int q = decltype(q_)::value;
+        if (q > 0) u[q] = cmul(u[q], cconj(tw[q * k1]));
+        ex[(k1 * P + q) * 32 + lane] = u[q];
+      });
+    }
+    __syncthreads();
+  }
+  __syncthreads();   // the exchange buffer is free again
+}
+
+template <typename T> constexpr bool kCompactFilter = std::is_same<T, dfloat>::value;
 
 // Column passes keep the Boltzmann-factor tile of their output (N rows x 64
 // floats) in shared memory after the twiddle/gain tables.
@@ -189,7 +258,8 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
     __syncthreads();   // the shared tables are complete
   }
 
-  four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
+  if constexpr (kCompactFilter<T>) four_step_compact<N, P>(v, ex, s_tw, s_g, p, lane);
+  else four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
 
   if constexpr (XP) {
     constexpr int PITCH = N + 1;
@@ -559,10 +629,9 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<T> ps) {
     });
   }
   __syncthreads();   // the shared tables are complete
-  four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
-  asm volatile("cp.async.wait_all;" ::: "memory");
-  __syncthreads();   // every thread's tile copies are visible
-  {
+  auto finish_step = [&]() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();   // every thread's tile copies are visible
     T *dq = qo + b * ps.qout_bs[set] + base;
     reg::static_for<0, R1>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
@@ -573,8 +642,19 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<T> ps) {
       *reinterpret_cast<C *>(dq + (long long)(p + P * j) * ap.s_n) = r;
       v[j] = mkc<C, T>(r.x * wv.x, r.y * wv.y);
     });
+  };
+  if constexpr (kCompactFilter<T>) {
+#pragma unroll 1
+    for (int half = 0; half < 2; ++half) {
+      four_step_compact<N, P>(v, ex, s_tw, s_g, p, lane);
+      if (half == 1) break;
+      finish_step();
+    }
+  } else {
+    four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
+    finish_step();
+    four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
   }
-  four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
   T *dst = out + b * ps.out_bs[set] + base;
   reg::static_for<0, R1>([&](auto j_) {
     constexpr int j = decltype(j_)::value;
@@ -647,12 +727,9 @@ __global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<T> ps) {
     });
     __syncthreads();
   };
-  rows_to_regs();
-  four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
-  regs_to_rows();
-  asm volatile("cp.async.wait_all;" ::: "memory");
-  __syncthreads();   // every thread's tile copies are visible
-  {
+  auto finish_step = [&]() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();   // every thread's tile copies are visible
     T *dq = ps.qout[set] + b * ps.qout_bs[set] + base;
 #pragma unroll 4
     for (int i = threadIdx.x; i < 64 * N; i += NT) {
@@ -662,11 +739,26 @@ __global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<T> ps) {
       dq[i] = x;
       stg[o] = x * w;
     }
+    __syncthreads();
+  };
+  if constexpr (kCompactFilter<T>) {
+#pragma unroll 1
+    for (int half = 0; half < 2; ++half) {
+      rows_to_regs();
+      four_step_compact<N, P>(v, ex, s_tw, s_g, p, lane);
+      regs_to_rows();
+      if (half == 1) break;
+      finish_step();
+    }
+  } else {
+    rows_to_regs();
+    four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
+    regs_to_rows();
+    finish_step();
+    rows_to_regs();
+    four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
+    regs_to_rows();
   }
-  __syncthreads();
-  rows_to_regs();
-  four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
-  regs_to_rows();
   T *dst = ps.out[set] + b * ps.out_bs[set] + base;
 #pragma unroll 4
   for (int i = threadIdx.x; i < 64 * N; i += NT) dst[i] = stg[(i / N) * PITCH + (i % N)];
