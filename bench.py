@@ -581,15 +581,20 @@ def run_ours(args):
         import ctypes as C
         dptr = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_double))
         out5 = np.empty(5)
-        e2e_steps = max(1, min(args.steps, 5))
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
+        e2e_steps = max(1, min(args.steps, 10))
+
+        def e2e_step():
             ctx._ck(ctx.lib.scft_set_field(ctx.h, pkg.FIELD_WA, dptr(hw_a)))
             ctx._ck(ctx.lib.scft_set_field(ctx.h, pkg.FIELD_WB, dptr(hw_b)))
             ctx._ck(ctx.lib.scft_iterate(ctx.h, 1, out5.ctypes.data_as(C.POINTER(C.c_double))))
             ctx._ck(ctx.lib.scft_get_field(ctx.h, pkg.FIELD_PHA, dptr(ho_a)))
             ctx._ck(ctx.lib.scft_get_field(ctx.h, pkg.FIELD_PHB, dptr(ho_b)))
+
+        e2e_step()                      # warm-up: first touch of the pinned buffers
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
         barrier()
         e2e_s = max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{dev}")
         e2e = {"value": ws * pt_steps * e2e_steps / e2e_s / 1e9, "unit": UNIT,
