@@ -43,6 +43,33 @@ def test_group_equals_individual(pkg, mixing):
         ctx.close()
 
 
+def test_group_mixes_precisions_and_rules(pkg):
+    """Members may differ in propagation precision (FP32, FP64, double-float)
+    and contour rule; each still reaches exactly its own solo result."""
+    members = [
+        dict(MEMBERS[0], precision=pkg.PREC_FP64),
+        dict(MEMBERS[2], precision=pkg.PREC_DF, flags=pkg.FLAG_SIMPSON),
+        dict(MEMBERS[3], precision=pkg.PREC_FP32, mixing=1, anderson_history=4),
+        dict(MEMBERS[3], nz=32, lz=4.0, precision=pkg.PREC_DF),
+    ]
+    solo = []
+    for i, kw in enumerate(members):
+        with pkg.Context(**kw) as ctx:
+            ctx.set_w(*start_fields(kw, i))
+            ctx.iterate(4)
+            solo.append((ctx.wb, ctx.phb))
+    ctxs = [pkg.Context(**kw) for kw in members]
+    for i, (ctx, kw) in enumerate(zip(ctxs, members)):
+        ctx.set_w(*start_fields(kw, i))
+    with pkg.Group(ctxs) as g:
+        g.iterate(4)
+    for ctx, (wb, phb) in zip(ctxs, solo):
+        assert np.array_equal(ctx.wb, wb)
+        assert np.array_equal(ctx.phb, phb)
+    for ctx in ctxs:
+        ctx.close()
+
+
 @pytest.mark.parametrize("grid", [(64, 64, 64), (128, 64, 32)])
 def test_autotuned_schedule_gives_same_results(pkg, grid):
     from scft_gb300 import fields
