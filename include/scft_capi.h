@@ -313,8 +313,9 @@ int scft_load_checkpoint(scft_ctx *ctx, const char *path);
  * also appends one line per instance,
  *   {"iteration":..,"instance":..,"F":..,"F_AB":..,"F_W":..,"F_S":..,
  *    "inCompMax":..,"residual_max":..,"residual_rms":..,"elapsed_s":..}
- * (residual: the mean-free max-norm and RMS of phi_w's update direction).
- * NULL or "" turns it off.  The file is opened for appending on each report. */
+ * (residual: the mean-free max-norm and RMS of phi_w's update direction;
+ * NaN or Inf is written as null).  NULL or "" turns it off.  The file is
+ * opened for appending on each report. */
 int scft_set_metrics_file(scft_ctx *ctx, const char *path);
 
 /* Read phi_<idx>.dat (init_cuda.cu:435-456) for instance `inst` of the

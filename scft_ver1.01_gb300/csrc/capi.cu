@@ -1114,7 +1114,10 @@ int scft_get_q(scft_ctx *ctx, int q, int s, double *dst) {
                                    M, ctx->batch, ctx->st));
     return SCFT_OK;
   });
-  if (rc) return rc;
+  if (rc) {
+    cudaFreeAsync(stage, ctx->st);
+    return rc;
+  }
   CK(cudaMemcpyAsync(dst, stage, sizeof(double) * M * ctx->batch, cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaFreeAsync(stage, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
@@ -1184,6 +1187,14 @@ int scft_set_metrics_file(scft_ctx *ctx, const char *path) {
 }
 
 namespace {
+// A JSON number (round-trip precision), or null for NaN/Inf (not JSON numbers).
+std::string json_num(double v) {
+  if (!std::isfinite(v)) return "null";
+  char b[32];
+  snprintf(b, sizeof b, "%.17g", v);
+  return b;
+}
+
 // One JSON line per instance for a progress report (scft_set_metrics_file).
 int write_metrics(scft_ctx *ctx, int iter, const double *fe, double elapsed_s) {
   std::vector<double> mx(ctx->batch), rms(ctx->batch);
@@ -1191,13 +1202,15 @@ int write_metrics(scft_ctx *ctx, int iter, const double *fe, double elapsed_s) {
   if (rc) return rc;
   FILE *fp = fopen(ctx->metrics_path.c_str(), "a");
   if (!fp) return scft_fail(ctx, SCFT_ERR_IO, "cannot append to " + ctx->metrics_path);
-  for (int i = 0; i < ctx->batch; ++i)
-    fprintf(fp,
-            "{\"iteration\":%d,\"instance\":%d,\"F\":%.17g,\"F_AB\":%.17g,\"F_W\":%.17g,"
-            "\"F_S\":%.17g,\"inCompMax\":%.17g,\"residual_max\":%.17g,"
-            "\"residual_rms\":%.17g,\"elapsed_s\":%.6f}\n",
-            iter, i, fe[5 * i + 0], fe[5 * i + 1], fe[5 * i + 2], fe[5 * i + 3], fe[5 * i + 4],
-            mx[i], rms[i], elapsed_s);
+  static const char *keys[5] = {"F", "F_AB", "F_W", "F_S", "inCompMax"};
+  for (int i = 0; i < ctx->batch; ++i) {
+    std::string line = "{\"iteration\":" + std::to_string(iter) +
+                       ",\"instance\":" + std::to_string(i);
+    for (int k = 0; k < 5; ++k) line += std::string(",\"") + keys[k] + "\":" + json_num(fe[5 * i + k]);
+    line += ",\"residual_max\":" + json_num(mx[i]) + ",\"residual_rms\":" + json_num(rms[i]) +
+            ",\"elapsed_s\":" + json_num(elapsed_s) + "}\n";
+    fputs(line.c_str(), fp);
+  }
   return fclose(fp) == 0 ? SCFT_OK : scft_fail(ctx, SCFT_ERR_IO, "write " + ctx->metrics_path);
 }
 }  // namespace
