@@ -291,8 +291,8 @@ const char *scft_noalloc_last_error(void);
  * After the reference's seven lines, optional `key=value` lines (one per
  * line, no reference counterpart) set: mixing=simple|anderson, history=<m>,
  * lambda=<Anderson step>, start=<Anderson switch residual>, wopt=, wcmp=,
- * precision=fp32|fp64|df, Ns=<contour steps> (ds0 = 1/Ns).  An unknown key or a
- * bad value is SCFT_ERR_IO. */
+ * precision=fp32|fp64|df, Ns=<contour steps> (ds0 = 1/Ns); lines starting
+ * with '#' are comments.  An unknown key or a bad value is SCFT_ERR_IO. */
 int scft_read_ab_txt(const char *path, scft_params *p, int *intag);
 
 /* ---- checkpoint / metrics (no reference counterpart) ---- */

@@ -36,7 +36,7 @@ int scft_read_ab_txt(const char *path, scft_params *p, int *intag) {
   while (fgets(line, sizeof line, fp)) {
     std::string l(line);
     while (!l.empty() && (l.back() == '\n' || l.back() == '\r' || l.back() == ' ')) l.pop_back();
-    if (l.empty()) continue;
+    if (l.empty() || l[0] == '#') continue;   // blank lines and comments
     const size_t eq = l.find('=');
     std::string err;
     if (eq == std::string::npos) {

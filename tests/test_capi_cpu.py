@@ -97,7 +97,7 @@ AB7 = ("intag=1024\nxN=25.0\nfa=0.300\nlx=4.2, ly=7.2746, lz=2.0\n"
 
 def test_read_ab_txt_optional_keys(pkg, tmp_path):
     f = tmp_path / "ab.txt"
-    f.write_text(AB7 + "mixing=anderson\nhistory=30\nlambda=0.4\nstart=0.5\n"
+    f.write_text(AB7 + "# solver options\nmixing=anderson\nhistory=30\nlambda=0.4\nstart=0.5\n"
                  "wopt=0.02\nwcmp=0.2\nprecision=fp32\nNs=400\n\n")
     p, tag = pkg.read_ab_txt(str(f))
     assert tag == 1024 and (p.nx, p.nz, p.batch) == (128, 64, 3)
