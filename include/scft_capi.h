@@ -42,7 +42,7 @@ extern "C" {
                                      numbers, ~48 significant bits) on the FP32 pipe, FP64
                                      elsewhere: FP64-level results faster than native FP64 on
                                      GB300; Nx of 64 or 128, Ny and Nz of 1, 32, 64 or 128,
-                                     Ny*Nz a multiple of 64; no adjoint or stress */
+                                     Ny*Nz a multiple of 64 */
 
 #define SCFT_FIELD_WA 0
 #define SCFT_FIELD_WB 1

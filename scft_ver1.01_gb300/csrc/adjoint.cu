@@ -149,8 +149,9 @@ __global__ void k_adj_q(const R *__restrict__ p, const R *__restrict__ lam,
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M;
        i += (long long)gridDim.x * blockDim.x) {
     const long long o = b * M + i, so = b * seg_bs + i;
-    const double l = lam[o], pp = p[o], q1 = qs[so], q0 = qsm1[so];
-    const double c1 = qcs[o], c0 = qcsm1[o];
+    const double l = (double)lam[o], pp = (double)p[o], q1 = (double)qs[so],
+                 q0 = (double)qsm1[so];
+    const double c1 = (double)qcs[o], c0 = (double)qcsm1[o];
     wbar[o] -= hds * (l * q1 + pp * q0);
     G[o] += c1 * q1 + c0 * q0;
     const double qq = q0 * c0;
@@ -174,7 +175,7 @@ __global__ void k_adj_qc(const R *__restrict__ p, const R *__restrict__ mu,
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M;
        i += (long long)gridDim.x * blockDim.x) {
     const long long o = b * M + i, so = b * seg_bs + i;
-    const double m = mu[o], pp = p[o];
+    const double m = (double)mu[o], pp = (double)p[o];
     wbar[o] -= hds * (m * (double)qcsm1[so] + pp * (double)qcs[so]);
     mu_out[o] = (R)(pp + ffl[b] * (cA * pbA[o] + cB * pbB[o]) * (double)qs[o]);
   }
@@ -564,8 +565,6 @@ int scft_adjoint(scft_ctx *ctx, const double *pha_bar, const double *phb_bar,
                  const double *Q_bar, double *wa_bar, double *wb_bar, double *L_bar,
                  int checkpoint_every) {
   if (!ctx) return SCFT_ERR_INVALID_ARG;
-  if (ctx->rkind == kRealDF)
-    return scft_fail(ctx, SCFT_ERR_UNSUPPORTED, "no adjoint for double-float contexts");
   const int N = ctx->NsA + ctx->dNsB;
   if (N < 1) return scft_fail(ctx, SCFT_ERR_UNSUPPORTED, "adjoint needs at least one step");
   if (checkpoint_every < 0) return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "bad checkpoint interval");
@@ -574,9 +573,9 @@ int scft_adjoint(scft_ctx *ctx, const double *pha_bar, const double *phb_bar,
   if (K > N) K = N;
   CK(cudaSetDevice(ctx->p.device));
   RC(ensure_adjoint(ctx, K));
-  return ctx->rbytes == 4 ? adjoint_impl<float>(ctx, pha_bar, phb_bar, Q_bar, wa_bar, wb_bar, L_bar)
-                          : adjoint_impl<double>(ctx, pha_bar, phb_bar, Q_bar, wa_bar, wb_bar,
-                                                 L_bar);
+  return with_real(ctx, [&](auto r) {
+    return adjoint_impl<decltype(r)>(ctx, pha_bar, phb_bar, Q_bar, wa_bar, wb_bar, L_bar);
+  });
 }
 
 int scft_adjoint_checkpoints(scft_ctx *ctx, int checkpoint_every, int *slices,
@@ -593,8 +592,6 @@ int scft_adjoint_checkpoints(scft_ctx *ctx, int checkpoint_every, int *slices,
 
 int scft_stress(scft_ctx *ctx, double *dF_dL) {
   if (!ctx || !dF_dL) return SCFT_ERR_INVALID_ARG;
-  if (ctx->rkind == kRealDF)
-    return scft_fail(ctx, SCFT_ERR_UNSUPPORTED, "no stress for double-float contexts");
   if (!ctx->have_conc)
     return scft_fail(ctx, SCFT_ERR_INVALID_ARG,
                      "no getConc at the current box: call scft_get_conc first");
@@ -613,7 +610,7 @@ int scft_stress(scft_ctx *ctx, double *dF_dL) {
     A.sbytes = A.sacc_off + 8 * ((size_t)4 * ctx->batch * ctx->nblk + 4 * ctx->batch);
     CK(cudaMalloc(&A.smem, A.sbytes));
   }
-  return ctx->rbytes == 4 ? stress_impl<float>(ctx, dF_dL) : stress_impl<double>(ctx, dF_dL);
+  return with_real(ctx, [&](auto r) { return stress_impl<decltype(r)>(ctx, dF_dL); });
 }
 
 int scft_relax_cell(scft_ctx *ctx, int axes_mask, double tol_w, double tol_stress,

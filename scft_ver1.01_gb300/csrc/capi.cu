@@ -778,15 +778,11 @@ int filter_impl(scft_ctx *ctx, const R *in, long long in_bs, R *out, long long o
 int scft_internal_filter(scft_ctx *ctx, const void *in, long long in_bs, void *out,
                          long long out_bs, const void *pre, const void *post, long long w_bs,
                          int nb, int deriv_pass, void *s0, void *s1, cudaStream_t st) {
-  if (ctx->rkind == kRealDF)
-    return scft_fail(ctx, SCFT_ERR_UNSUPPORTED, "no adjoint or stress for double-float contexts");
-  if (ctx->rbytes == 4)
-    return filter_impl<float>(ctx, (const float *)in, in_bs, (float *)out, out_bs,
-                              (const float *)pre, (const float *)post, w_bs, nb, deriv_pass,
-                              (float *)s0, (float *)s1, st);
-  return filter_impl<double>(ctx, (const double *)in, in_bs, (double *)out, out_bs,
-                             (const double *)pre, (const double *)post, w_bs, nb, deriv_pass,
-                             (double *)s0, (double *)s1, st);
+  return with_real(ctx, [&](auto r) {
+    using R = decltype(r);
+    return filter_impl<R>(ctx, (const R *)in, in_bs, (R *)out, out_bs, (const R *)pre,
+                          (const R *)post, w_bs, nb, deriv_pass, (R *)s0, (R *)s1, st);
+  });
 }
 
 int scft_fail(scft_ctx *ctx, int status, const std::string &msg) {

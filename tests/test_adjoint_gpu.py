@@ -114,6 +114,36 @@ def test_adjoint_with_simpson_weights(pkg, orc, fA):
     assert abs(float(gL[:, 0].sum()) - fd) < 2e-6 * max(abs(fd), 1e-3)
 
 
+def test_double_float_stress_and_adjoint(pkg, orc):
+    """SCFT_PREC_DF: the stress at FP64 level (the oracle's spectral formula)
+    and the adjoint against central differences, on a grid with register
+    kernels on every axis."""
+    case = (64, 32, 32, 4.1, 3.3, 2.9, 0.4, 0.05)
+    ctx, p = make(pkg, orc, case, prec=pkg.PREC_DF)
+    rng = np.random.default_rng(13)
+    wa, wb = fields(p.shape, 2, 8, scale=1.0)
+    pbA = rng.normal(0, 1, wa.shape)
+    pbB = rng.normal(0, 1, wa.shape)
+    Qb = rng.normal(0, 1, 2)
+    with ctx:
+        ctx.set_w(wa, wb)
+        ctx.get_conc()
+        sig = ctx.stress()
+        gA, gB, gL = ctx.adjoint(pbA, pbB, Qb)
+    assert rel(sig, orc.stress_spectral(wa, wb, p)) < 1e-9
+    J = lambda a, b, pp: orc.conc_functional(a, b, pp, pbA, pbB, Qb)
+    dA = rng.normal(0, 1, wa.shape)
+    dB = rng.normal(0, 1, wa.shape)
+    h = 1e-5
+    fd = (J(wa + h * dA, wb + h * dB, p) - J(wa - h * dA, wb - h * dB, p)) / (2 * h)
+    ad = float((gA * dA).sum() + (gB * dB).sum())
+    assert abs(ad - fd) < 2e-6 * max(abs(fd), 1e-3), (ad, fd)
+    h = 1e-4 * p.ly
+    fd = (J(wa, wb, orc.with_box(p, p.lx, p.ly + h, p.lz))
+          - J(wa, wb, orc.with_box(p, p.lx, p.ly - h, p.lz))) / (2 * h)
+    assert abs(float(gL[:, 1].sum()) - fd) < 2e-6 * max(abs(fd), 1e-3)
+
+
 def test_dlnQ_dw_is_minus_phi_over_M(pkg, orc):
     ctx, p = make(pkg, orc, CASES[0])
     with ctx:
