@@ -398,6 +398,28 @@ def stress_leg(pkg, dev, relax=False, budget_s=60.0):
         out["stress_fd_fp64_h1e-4L"] = fd
         out["rel_err_fp64_vs_fd"] = max(abs(a - b) for a, b in zip(s64[0], fd)) / den
         out["rel_err_fp32_vs_fp64"] = max(abs(a - b) for a, b in zip(s32[0], s64[0])) / den
+        # the same stress at FP64 level in double-float arithmetic, and the
+        # getConc + stress time of each precision at these fields
+        c.set_box(lx, ly, lz)
+        c.set_w(wa1, wb1)
+        c.synchronize()
+        t0 = time.perf_counter()
+        c.get_conc()
+        c.stress()
+        t_prec = {"fp64": (time.perf_counter() - t0) * 1e3}
+    with pkg.Context(precision=pkg.PREC_DF, **kw) as c:
+        c.set_w(wa1, wb1)
+        c.get_conc()
+        c.stress()                       # warm-up (tables, buffers)
+        c.set_w(wa1, wb1)
+        c.synchronize()
+        t0 = time.perf_counter()
+        c.get_conc()
+        sdf = c.stress()
+        t_prec["df"] = (time.perf_counter() - t0) * 1e3
+        out["stress_df"] = sdf[0].tolist()
+        out["rel_err_df_vs_fp64"] = max(abs(a - b) for a, b in zip(sdf[0], s64[0])) / den
+        out["getconc_plus_stress_ms"] = t_prec
     if relax:
         with pkg.Context(precision=pkg.PREC_FP32, **kw) as c:
             c.set_w(wa1, wb1)
