@@ -1,4 +1,8 @@
-// Register-resident per-axis line filter (FP32), the fast propagator pass.
+// Register-resident line filters, the fast propagator passes: per-axis
+// passes (k_fast_line), x+y planes (k_xy_plane), fused step pairs (k_xyxy,
+// k_zz, k_xx) and a pipelined column pass (k_col_pipe).  The real type is
+// FP32, FP64 or the double-float pair (dfloat.cuh) where a kernel is
+// templated on it; the plane kernels and the pipelined pass are FP32.
 //
 // Same operator as k_line.cu (one axis of the separable split step
 // exp(-k^2 ds)/N), organised as a four-step FFT with compile-time N = P*R1:
@@ -9,9 +13,9 @@
 //   stage 2 (registers):   per k1 owned by the warp: DFT_P over p -> X[k1+R1*k2],
 //                          multiply by the gain, inverse DFT_P, twiddle W_N^(-p*k1)
 //   exchange back, inverse DFT_R1 over k1 -> natural order.
-// Column passes (lines along y or z, stride s_n) load float2 straight from
-// global memory: the 32 lanes of a warp read 64 consecutive x values (256 B,
-// coalesced) per element.  The x pass stages a 64-row tile through shared
+// Column passes (lines along y or z, stride s_n) load complex pairs straight
+// from global memory: the 32 lanes of a warp read 64 consecutive x values
+// (256 B in FP32, coalesced) per element.  The x pass stages a 64-row tile through shared
 // memory (row pitch N+1 floats, conflict-free) and packs rows (l, l+32).
 // The Boltzmann factor of the split step is applied on load (pre) and on
 // store (post), so q makes one round trip per pass.
