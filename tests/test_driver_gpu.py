@@ -99,6 +99,29 @@ def test_driver_optional_keys_and_metrics(pkg, orc, tmp_path):
     assert simple[-1]["residual_max"] > rows[-1]["residual_max"]
 
 
+def test_driver_double_float(pkg, orc, tmp_path):
+    """-precision=df: FP32-pair propagation gives the oracle's progress lines
+    to the 9 digits the line prints."""
+    from scft_gb300 import fields
+    p = orc.Params(nx=64, ny=32, nz=32, lx=4.0, ly=3.0, lz=3.0, hAB=20.0, fA=0.5, ds0=0.02,
+                   batch=1)
+    wa, wb = fields.lamellar(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 20.0, seed=6, batch=1)
+    d = str(tmp_path)
+    write_case(orc, d, p, wa, wb)
+    r = subprocess.run([DRIVER, "-step=20", "-precision=df"], cwd=d, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = [l for l in r.stdout.splitlines() if l.startswith("GPU ")]
+    assert len(lines) == 2
+    wa0 = orc.read_phi_dat(os.path.join(d, "phi_1.dat"), p.M)[2].reshape((1,) + p.shape)
+    wb0 = orc.read_phi_dat(os.path.join(d, "phi_1.dat"), p.M)[3].reshape((1,) + p.shape)
+    ref = orc.free_loop(wa0, wb0, p, 20)
+    for l, row in zip(lines, ref.log):
+        it, b, F, fab, fw, fs, inc = row
+        vals = [float(v) for v in l.split(":")[2].split(",")]
+        np.testing.assert_allclose(vals[:4], [F, fab, fw, fs], rtol=2e-8, atol=1e-12)
+
+
 def test_driver_missing_config(pkg, tmp_path):
     r = subprocess.run([DRIVER, "-step=1"], cwd=str(tmp_path), capture_output=True, text=True,
                        timeout=120)
