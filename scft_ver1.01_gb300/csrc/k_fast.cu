@@ -891,8 +891,26 @@ template <typename T, int N, int P, bool XP> size_t fast_smem() {
             : fast_wtile_off<T, N, XP>() + (size_t)N * 64 * sizeof(T);
 }
 
+// Host-side shape checks of the tiled launches (the sanitizer substitute):
+// the kernel's compile-time line length matches the plan, the 64-line tiles
+// cover the lines exactly, and the grid fits CUDA's limits.  A failed check
+// is an error status, never a launch.
+template <typename T>
+bool tiles_ok(const AxisPlan &ap, int n, bool outer_in_y, const PassSet<T> &ps) {
+  const long long sets = (long long)ps.nset * ps.batch;
+  return ap.n == n && ap.n_real > 0 && ap.n_real % 64 == 0 && sets >= 1 && sets <= 65535 &&
+         (!outer_in_y || (ap.n_outer >= 1 && ap.n_outer <= 65535));
+}
+inline bool planes_ok(const AxisPlan &apx, const AxisPlan &apy, int nx, int ny,
+                      const PassSet<float> &ps) {
+  const long long sets = (long long)ps.nset * ps.batch;
+  return apx.n == nx && apy.n == ny && apy.s_n == nx && apy.n_outer >= 1 && sets >= 1 &&
+         sets <= 65535;
+}
+
 template <typename T, int N, int P, bool XP>
 cudaError_t launch_one(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
+  if (!tiles_ok(ap, N, !XP, ps)) return cudaErrorInvalidValue;
   dim3 grid(ap.n_real / 64, XP ? 1 : ap.n_outer, ps.nset * ps.batch);
   return launch_pdl(k_fast_line<T, N, P, XP>, grid, dim3(P * 32), fast_smem<T, N, P, XP>(), st,
                     ap, ps);
@@ -954,6 +972,7 @@ template <int NX, int NY> cudaError_t prep_xy() {
 template <int NX, int NY>
 cudaError_t launch_xy_t(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
                         cudaStream_t st) {
+  if (!planes_ok(apx, apy, NX, NY, ps)) return cudaErrorInvalidValue;
   constexpr int G = xy_groups<NX, NY>();
   dim3 grid(apy.n_outer, 1, ps.nset * ps.batch);   // one CTA per z-plane
   return launch_pdl(k_xy_plane<NX, NY, G>, grid, dim3(256 * G), xy_smem<NX, NY, G>(), st, apx,
@@ -967,6 +986,7 @@ template <int NX, int NY> cudaError_t prep_xyxy() {
 template <int NX, int NY>
 cudaError_t launch_xyxy_t(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
                           cudaStream_t st) {
+  if (!planes_ok(apx, apy, NX, NY, ps)) return cudaErrorInvalidValue;
   constexpr int G = xy_groups<NX, NY>();
   dim3 grid(apy.n_outer, 1, ps.nset * ps.batch);   // one CTA per z-plane
   return launch_pdl(k_xyxy<NX, NY, G>, grid, dim3(256 * G), xyxy_smem<NX, NY, G>(), st, apx,
@@ -978,6 +998,7 @@ template <typename T, int N, int P> cudaError_t prep_xx() {
 }
 template <typename T, int N, int P>
 cudaError_t launch_xx_t(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
+  if (!tiles_ok(ap, N, false, ps)) return cudaErrorInvalidValue;
   dim3 grid(ap.n_real / 64, 1, ps.nset * ps.batch);
   return launch_pdl(k_xx<T, N, P>, grid, dim3(P * 32), xx_smem<T, N>(), st, ap, ps);
 }
@@ -987,6 +1008,7 @@ template <typename T, int N, int P> cudaError_t prep_zz() {
 }
 template <typename T, int N, int P>
 cudaError_t launch_zz_t(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
+  if (!tiles_ok(ap, N, true, ps)) return cudaErrorInvalidValue;
   dim3 grid(ap.n_real / 64, ap.n_outer, ps.nset * ps.batch);
   return launch_pdl(k_zz<T, N, P>, grid, dim3(P * 32), fast_smem<T, N, P, false>(), st, ap,
                     ps);
