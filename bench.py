@@ -145,6 +145,36 @@ def cpu_baseline(seconds=12.0):
                       f"FP64, {workers} threads), {done_s:.1f} s"}
 
 
+def reference_cuda_leg(iters=2):
+    """The reference's own CUDA build on this GPU: its kernels (cuda_aid.cu,
+    compiled unchanged for sm_103a into oracle/_ref/ref_kernels.cubin) driven
+    in its host order with cuFFT D2Z/Z2D in FP64 (oracle/ref_harness.cpp), on
+    the benchmark workload; timed as its fft_test times Free
+    (cuda_scft.cu:411-425): events around whole SCF iterations."""
+    try:
+        from oracle import ref_harness
+        if not ref_harness.available():
+            return {"unavailable": "oracle/_ref (the reference kernels + harness) not built"}
+        import __graft_entry__ as ge
+        ge.load_package()
+        from scft_gb300 import fields as fl
+        wa, wb = fl.gyroid(N, N, N, L, L, L, CHIN, seed=0)
+        r = ref_harness.RefSolver(N, N, N, L, L, L, CHIN, FA, DS, 1)
+        r.set_q_mode(0)           # exactly as it runs (its cal_ql kernel)
+        r.set_w(wa, wb)
+        r.iterate(1, with_energy=False)        # warm-up: plans, module load
+        ms = r.time_iterations(iters) / iters
+        pts = 2 * (r.NsA + r.dNsB) * N ** 3
+        r.close()
+        return {"what": "the reference's kernels (unchanged, sm_103a) + cuFFT FP64 in its host "
+                        "order, one GB300, 128^3 gyroid Ns=200, CUDA events around %d SCF "
+                        "iterations" % iters,
+                "ms_per_iteration": ms, "value": pts / (ms / 1e3) / 1e9, "unit": UNIT,
+                "dtype": "f64"}
+    except Exception as e:                     # no GPU or harness failure: say so
+        return {"unavailable": str(e).splitlines()[0][:200]}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -178,6 +208,7 @@ def run_reference(args):
                                    f"so its algorithm runs as the CPU restatement with "
                                    f"scipy.fft on {workers} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_cuda": reference_cuda_leg() if not args.no_ref_cuda else None,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -469,6 +500,27 @@ def large_leg(pkg, dev, converge=False, budget_s=120.0):
     return out
 
 
+def precision_matched_leg(pkg, dev, iters=3):
+    """The FP64-level paths on the benchmark workload (128^3 gyroid, Ns=200,
+    simple mixing): plain FP64 and double-float (FP32-pair) propagation, in
+    Gpt*step/s from device events around whole SCF iterations, for comparison
+    with the reference's FP64 CUDA build at the same arithmetic accuracy."""
+    from scft_gb300 import fields as fl
+    wa, wb = fl.gyroid(N, N, N, L, L, L, CHIN, seed=0)
+    out = {"what": "128^3 gyroid Ns=200, 1 SCF iteration per step, %d steps after a warm-up"
+                   % iters}
+    for name, prec in (("fp64", pkg.PREC_FP64), ("df", pkg.PREC_DF)):
+        with pkg.Context(nx=N, ny=N, nz=N, lx=L, ly=L, lz=L, hAB=CHIN, fA=FA, ds0=DS,
+                         precision=prec, device=dev) as c:
+            c.set_w(wa, wb)
+            c.iterate(2)
+            c.synchronize()
+            ms = c.time_iterations(iters) / iters
+            pts = 2 * (c.NsA + c.dNsB) * N ** 3
+            out[name] = {"ms_per_iteration": ms, "gpt_step_per_s": pts / (ms / 1e3) / 1e9}
+    return out
+
+
 def cufft_leg(dev, n=N, steps=50):
     """cuFFT comparison (timed only as a comparison, not used by the library):
     the same FP32 split step q <- W*irfftn(G*rfftn(W*q)) with torch.fft
@@ -641,9 +693,11 @@ def run_ours(args):
             "config": {"workload": workload, "grid": [n, n, n], "Ns": args.ns, "batch": 1,
                        "propagation": args.precision,
                        "reductions": "fp64 (Q, F, mixing); phi contour sum compensated",
-                       "l2": "inputs larger than L2: each step streams %.1f GB of propagator "
-                             "slices through HBM" % (4 * (ctx.NsA + ctx.dNsB + 2) * n ** 3 *
-                                                     (4 if args.precision == "fp32" else 8) / 1e9),
+                       "l2": "inputs larger than L2: each step (one SCF iteration) stores "
+                             "and re-reads %.1f GB of propagator slices (2*(NsA+dNsB+2) slices "
+                             "of the four marches) through HBM"
+                             % (2 * (ctx.NsA + ctx.dNsB + 2) * n ** 3 *
+                                (4 if args.precision == "fp32" else 8) / 1e9),
                        "parallelism": f"replicas x{ws} (no exchange step)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
@@ -671,6 +725,8 @@ def run_ours(args):
                                if (not args.no_stress and ws == 1) else None),
             "cufft_comparison": (cufft_leg(dev) if (headline and ws == 1 and not args.no_cufft)
                                  else None),
+            "precision_matched": (precision_matched_leg(pkg, dev)
+                                  if (headline and ws == 1 and not args.no_prec) else None),
             "large_256": (large_leg(pkg, dev, converge=args.large_converge)
                           if (headline and ws == 1 and not args.no_large) else None),
         }
@@ -702,6 +758,10 @@ def main():
                     help="skip the config-3 stress / adjoint leg")
     ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT comparison leg")
     ap.add_argument("--no-large", action="store_true", help="skip the 256^3 Ns=400 leg")
+    ap.add_argument("--no-prec", action="store_true",
+                    help="skip the FP64 / double-float rates at 128^3")
+    ap.add_argument("--no-ref-cuda", action="store_true",
+                    help="reference arm: skip the reference's own CUDA build")
     ap.add_argument("--large-converge", action="store_true",
                     help="add the 256^3 convergence run to the large leg (minutes)")
     ap.add_argument("--relax", action="store_true",

@@ -3,9 +3,12 @@
  * struct.h:19-125 of ren5885a/SCFT_Ver1.01) re-declared for the GB300 build,
  * so a driver written against the reference compiles unchanged.  Field names
  * and meanings are kept; the implementation behind them is the C ABI of
- * ../scft_capi.h (one GPU: the reference's GPU_N split collapses to one
- * device).  Differences a caller can observe:
- *   - the *_cu vectors hold one device pointer each (index 0);
+ * ../scft_capi.h.  -GPU_N / -gpu<i> split the instances over devices as the
+ * reference does (batch = Num_SCFT / GPU_N per device, init_cuda.cu:312), one
+ * context per device, with no data moving between them.  Differences a
+ * caller can observe:
+ *   - the *_cu vectors hold one device pointer per shard (index gpu_index),
+ *     as the reference's do;
  *   - wa_cu/wb_cu/pha_cu/phb_cu are FP64 [batch][Nz][Ny][Nx] device arrays;
  *   - qa_cu/qb_cu/qca_cu/qcb_cu point at contour-outer propagator storage
  *     ([batch][s][Nz][Ny][Nx] in the propagation precision: FP64, FP32, or
@@ -95,6 +98,9 @@ typedef struct {
   scft_params opts = {};
   /* -metrics=<path>: JSON-lines progress reports (scft_set_metrics_file) */
   char metrics[256] = {};
+  /* the contexts of the GPU_N split, one per listed device (gb300 == shard[0]) */
+  scft_ctx *shard[SCFT_MAX_SHARDS] = {};
+  int n_shard = 0;
 } CUFFT_INFO;
 
 #endif

@@ -201,6 +201,23 @@ int scft_iterate(scft_ctx *ctx, int n_iter, double *out5);
  * SCFT_ERR_NOT_FINITE if F becomes NaN/Inf. */
 int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir);
 
+/* ---- instances split over several devices (GPU_N / -gpu<i>) ---- */
+#define SCFT_MAX_SHARDS 64
+/* The reference's split of Num_SCFT instances over gpu_n devices
+ * (init_cuda.cu:312, cufft_info->batch = Num_SCFT / GPU_N): every device gets
+ * *batch_per_gpu instances; the last *not_run (= Num_SCFT % GPU_N, may be
+ * NULL) are read but never run, as in the reference.  Host only.  Fewer
+ * instances than devices is SCFT_ERR_INVALID_ARG. */
+int scft_shard_plan(int num_scft, int gpu_n, int *batch_per_gpu, int *not_run);
+/* Free (cuda_scft.cu:140-269) over n shards, one context per device (each
+ * created with its device in scft_params.device and the same batch): shard g
+ * holds global instances g*batch .. g*batch+batch-1.  Every iteration is
+ * queued on all shards before any is waited for, so the devices run
+ * concurrently; no data moves between them.  Progress lines read
+ * "GPU <g> batch <i>" and files pha_<g*batch+i+1>.dat, the reference's
+ * order and numbering.  scft_free(ctx, ...) is the n == 1 case. */
+int scft_free_shards(scft_ctx *const *ctxs, int n, int max_it, int aver_it, const char *outdir);
+
 /* Wait for all work queued on the context's stream. */
 int scft_synchronize(scft_ctx *ctx);
 
@@ -266,8 +283,8 @@ long long scft_group_launch_count(const scft_group *g);
 /* ---- split step without device allocation ----
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * where they advance a propagator: a framework that owns all device memory
- * through its own pool, code running while a stream is captured into a CUDA
- * graph, or loops that cannot afford cudaMalloc's implicit synchronisation.
+ * through its own pool, or loops that cannot afford cudaMalloc's implicit
+ * synchronisation.
  * One FP32 split step q_out = W . IFFT[G . FFT[W . q_in]] / M (one contour
  * step of sovDifFft, cuda_scft.cu:467-491) for `batch` instances laid out
  * [batch][Nz][Ny][Nx]; q_in, W and q_out are caller-owned, 16-byte aligned
@@ -275,10 +292,13 @@ long long scft_group_launch_count(const scft_group *g);
  * exp(-w*ds0/2)), enqueued on
  * `stream` (a cudaStream_t; NULL = default stream).  Scratch lives in a static
  * device array of this library: batch*Nx*Ny*Nz is limited to 2^21 points
- * (larger requests return SCFT_ERR_INVALID_ARG), every GPU that loads the
+ * and batch to 65535 (larger requests return SCFT_ERR_INVALID_ARG before
+ * anything is enqueued), every GPU that loads the
  * library holds the array (~16 MB) until exit, and calls that overlap on the
  * GPU race on it.  The first call on a device looks up the array's address;
- * make it before any stream capture.  Never calls cudaMalloc/cudaFree. */
+ * make it before any stream capture.  A returned error is this call's own
+ * (an earlier, unrelated CUDA error does not fail it).  Never calls
+ * cudaMalloc/cudaFree. */
 int scft_split_step_noalloc(int nx, int ny, int nz, double lx, double ly, double lz, double ds0,
                             int batch, const float *q_in, const float *W, float *q_out,
                             void *stream);

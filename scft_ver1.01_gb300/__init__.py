@@ -45,6 +45,7 @@ EXPORTS = [
     "scft_adjoint_checkpoints", "scft_relax_cell", "scft_get_box", "scft_field_device_ptr",
     "scft_get_stream", "scft_copy_q_reference_layout", "scft_selftest_bounded_wait", "scft_spline", "scft_spline_eval",
     "scft_spline_deriv", "scft_spline_integral", "scft_spline_eval_device",
+    "scft_shard_plan", "scft_free_shards",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
 FLAG_AUTOTUNE, FLAG_NO_FUSED_STEPS, FLAG_SIMPSON = 32, 64, 128
@@ -104,6 +105,9 @@ def load_library(path: str | None = None):
         "scft_free_energy": (C.c_int, [vp, dp]),
         "scft_iterate": (C.c_int, [vp, C.c_int, dp]),
         "scft_free": (C.c_int, [vp, C.c_int, C.c_int, C.c_char_p]),
+        "scft_shard_plan": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int)]),
+        "scft_free_shards": (C.c_int, [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.c_char_p]),
         "scft_synchronize": (C.c_int, [vp]),
         "scft_launch_count": (C.c_longlong, [vp]),
         "scft_read_ab_txt": (C.c_int, [C.c_char_p, C.POINTER(ScftParams), C.POINTER(C.c_int)]),
@@ -162,6 +166,28 @@ def load_library(path: str | None = None):
     if path is None:
         _lib = lib
     return lib
+
+
+def shard_plan(num_scft: int, gpu_n: int):
+    """The reference's split of Num_SCFT instances over GPU_N devices
+    (init_cuda.cu:312): -> (instances per device, instances not run)."""
+    lib = load_library()
+    b, nr = C.c_int(), C.c_int()
+    st = lib.scft_shard_plan(num_scft, gpu_n, C.byref(b), C.byref(nr))
+    if st != OK:
+        raise ScftError(st, lib.scft_last_error(None).decode())
+    return b.value, nr.value
+
+
+def free_shards(ctxs, max_it: int, aver_it: int = 10, outdir: str | None = None):
+    """Free over contexts holding consecutive instance shards (one per
+    device): scft_free_shards."""
+    lib = load_library()
+    arr = (C.c_void_p * len(ctxs))(*[c.h for c in ctxs])
+    st = lib.scft_free_shards(arr, len(ctxs), max_it, aver_it,
+                              outdir.encode() if outdir else None)
+    if st != OK:
+        raise ScftError(st, lib.scft_last_error(ctxs[0].h).decode())
 
 
 def default_params(**kw) -> ScftParams:

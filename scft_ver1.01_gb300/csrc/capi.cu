@@ -1191,8 +1191,10 @@ std::string json_num(double v) {
   return b;
 }
 
-// One JSON line per instance for a progress report (scft_set_metrics_file).
-int write_metrics(scft_ctx *ctx, int iter, const double *fe, double elapsed_s) {
+// One JSON line per instance for a progress report (scft_set_metrics_file);
+// `first` is the global number of the context's instance 0 (its shard's
+// offset when instances are split over several devices).
+int write_metrics(scft_ctx *ctx, int iter, const double *fe, double elapsed_s, int first) {
   std::vector<double> mx(ctx->batch), rms(ctx->batch);
   int rc = scft_get_residual(ctx, mx.data(), rms.data());
   if (rc) return rc;
@@ -1201,7 +1203,7 @@ int write_metrics(scft_ctx *ctx, int iter, const double *fe, double elapsed_s) {
   static const char *keys[5] = {"F", "F_AB", "F_W", "F_S", "inCompMax"};
   for (int i = 0; i < ctx->batch; ++i) {
     std::string line = "{\"iteration\":" + std::to_string(iter) +
-                       ",\"instance\":" + std::to_string(i);
+                       ",\"instance\":" + std::to_string(first + i);
     for (int k = 0; k < 5; ++k) line += std::string(",\"") + keys[k] + "\":" + json_num(fe[5 * i + k]);
     line += ",\"residual_max\":" + json_num(mx[i]) + ",\"residual_rms\":" + json_num(rms[i]) +
             ",\"elapsed_s\":" + json_num(elapsed_s) + "}\n";
@@ -1211,36 +1213,83 @@ int write_metrics(scft_ctx *ctx, int iter, const double *fe, double elapsed_s) {
 }
 }  // namespace
 
-int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir) {
-  if (!ctx || max_it < 0 || aver_it < 1) return SCFT_ERR_INVALID_ARG;
-  std::vector<double> fe(5 * ctx->batch);
+// init_cuda.cu:312: cufft_info->batch = Num_SCFT / GPU_N.  The reference's
+// integer split: every device gets the same count, and the last
+// Num_SCFT % GPU_N instances (read from their phi_<i>.dat) are never run.
+int scft_shard_plan(int num_scft, int gpu_n, int *batch_per_gpu, int *not_run) {
+  if (!batch_per_gpu || gpu_n < 1 || gpu_n > SCFT_MAX_SHARDS || num_scft < 1)
+    return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad instance or device count");
+  if (num_scft < gpu_n)
+    return scft_fail(nullptr, SCFT_ERR_INVALID_ARG,
+                     "fewer instances than devices: the split would leave a device with none");
+  *batch_per_gpu = num_scft / gpu_n;
+  if (not_run) *not_run = num_scft % gpu_n;
+  return SCFT_OK;
+}
+
+// Free (cuda_scft.cu:140-269) over instances split across devices
+// (init_cuda.cu:312): shard g holds global instances g*batch .. g*batch +
+// batch-1.  Each iteration is enqueued on every shard's own stream before any
+// shard is waited for, so the devices run concurrently; nothing is exchanged
+// between them.  Progress lines and pha_<i>.dat files come out in the
+// reference's order (shard by shard, instance by instance) with its numbering.
+int scft_free_shards(scft_ctx *const *ctxs, int n, int max_it, int aver_it, const char *outdir) {
+  if (!ctxs || n < 1 || n > SCFT_MAX_SHARDS || max_it < 0 || aver_it < 1)
+    return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad shard list or iteration counts");
+  for (int g = 0; g < n; ++g)
+    if (!ctxs[g] || ctxs[g]->batch != ctxs[0]->batch)
+      return scft_fail(nullptr, SCFT_ERR_INVALID_ARG,
+                       "every shard needs a context with the same instance count");
+  const int batch = ctxs[0]->batch;
+  std::vector<double> fe(5 * (size_t)batch);
   const auto t0 = std::chrono::steady_clock::now();
   int iter = 0;
   do {                                   // cuda_scft.cu:167-253
     iter = iter + 1;
-    int rc = iterate_once(ctx);
-    if (rc) return rc;
-    if (iter % aver_it == 0) {
+    for (int g = 0; g < n; ++g) {
+      scft_ctx *ctx = ctxs[g];
+      if (cudaSetDevice(ctx->p.device) != cudaSuccess)
+        return scft_fail(ctx, SCFT_ERR_CUDA, "cudaSetDevice failed");
+      if (int rc = iterate_once(ctx)) return rc;
+    }
+    if (iter % aver_it != 0) continue;
+    for (int g = 0; g < n; ++g) {
+      scft_ctx *ctx = ctxs[g];
+      cudaSetDevice(ctx->p.device);
+      int rc;
       if ((rc = free_energy_dev(ctx))) return rc;
       if ((rc = read_fe(ctx, fe.data()))) return rc;
-      for (int i = 0; i < ctx->batch; ++i)
-        printf("GPU %d batch %d: %5d : %.8e, %.8e, %.8e,%.8e, %.8e\n", 0, i, iter, fe[5 * i + 0],
+      for (int i = 0; i < batch; ++i)
+        printf("GPU %d batch %d: %5d : %.8e, %.8e, %.8e,%.8e, %.8e\n", g, i, iter, fe[5 * i + 0],
                fe[5 * i + 1], fe[5 * i + 2], fe[5 * i + 3], fe[5 * i + 4]);
       fflush(stdout);
       if (!ctx->metrics_path.empty()) {
         const double el =
             std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        if ((rc = write_metrics(ctx, iter, fe.data(), el))) return rc;
+        if ((rc = write_metrics(ctx, iter, fe.data(), el, g * batch))) return rc;
       }
-      if (outdir && iter % (aver_it * 10) == 0) {
-        for (int i = 0; i < ctx->batch; ++i) {
-          std::string path = std::string(outdir) + "/pha_" + std::to_string(i + 1) + ".dat";
-          if ((rc = scft_write_pha_dat(ctx, path.c_str(), i))) return rc;
+    }
+    if (outdir && iter % (aver_it * 10) == 0) {
+      for (int g = 0; g < n; ++g) {
+        cudaSetDevice(ctxs[g]->p.device);
+        for (int i = 0; i < batch; ++i) {
+          std::string path =
+              std::string(outdir) + "/pha_" + std::to_string(g * batch + i + 1) + ".dat";
+          if (int rc = scft_write_pha_dat(ctxs[g], path.c_str(), i)) return rc;
         }
       }
     }
   } while (iter < max_it);
+  for (int g = 0; g < n; ++g) {
+    cudaSetDevice(ctxs[g]->p.device);
+    if (int rc = sync_check(ctxs[g])) return rc;
+  }
   return SCFT_OK;
+}
+
+int scft_free(scft_ctx *ctx, int max_it, int aver_it, const char *outdir) {
+  if (!ctx || max_it < 0 || aver_it < 1) return SCFT_ERR_INVALID_ARG;
+  return scft_free_shards(&ctx, 1, max_it, aver_it, outdir);
 }
 
 int scft_synchronize(scft_ctx *ctx) {

@@ -1,16 +1,19 @@
 // The reference's C++ driver/struct API (include/compat/*.h) implemented on
 // the C ABI, so the reference's driver (main.cpp:20-41) links against this
-// library unchanged.  One GPU: the reference's GPU_N split of `batch`
-// (init_cuda.cu:312) collapses onto the first listed device.  Errors print a
-// message and leave the structs in a state finalize_cufft accepts; nothing
-// calls exit() except init_scft on an unreadable ab.txt, where the reference
-// itself would crash (init.cpp:81-86).
+// library unchanged.  -GPU_N / -gpu<i> split the instances over devices as
+// the reference does (init_cuda.cu:312): one context (shard) per listed
+// device, each holding Num_SCFT / GPU_N instances, every call applied to all
+// shards, no data moving between devices.  Errors print a message and leave
+// the structs in a state finalize_cufft accepts; nothing calls exit() except
+// init_scft on an unreadable ab.txt, where the reference itself would crash
+// (init.cpp:81-86).
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <strings.h>
 
+#include <chrono>
 #include <string>
 
 #include "compat/cuda_scft.h"
@@ -46,11 +49,18 @@ int field_of(CUFFT_INFO *c, double *p) {
   if (!c->wb_cu.empty() && p == c->wb_cu[0]) return SCFT_FIELD_WB;
   return -1;
 }
-// Refresh the reference-layout mirror of propagator q (no-op without them).
-void refresh_mirror(CUFFT_INFO *c, int q) {
+// Refresh shard g's reference-layout mirror of propagator q (no-op without them).
+void refresh_mirror(CUFFT_INFO *c, int g, int q) {
   if (!c->reference_layout) return;
   std::vector<double *> *mir[4] = {&c->qa_cu, &c->qcb_cu, &c->qb_cu, &c->qca_cu};
-  report(c->gb300, scft_copy_q_reference_layout(c->gb300, q, (*mir[q])[0]), "reference layout");
+  report(c->shard[g], scft_copy_q_reference_layout(c->shard[g], q, (*mir[q])[g]),
+         "reference layout");
+}
+
+// Make shard g's device current (each shard's calls run on its own device).
+scft_ctx *use_shard(CUFFT_INFO *c, int g) {
+  cudaSetDevice(c->shard[g]->p.device);
+  return c->shard[g];
 }
 
 int prop_of(CUFFT_INFO *c, double *p) {
@@ -138,15 +148,20 @@ int init_scft(CUFFT_INFO *cufft_info, GPU_INFO *gpu_info, int argc, char **argv)
   return 0;
 }
 
-// init_cuda.cu:227-294 (device selection; peer access is not needed)
+// init_cuda.cu:227-294 (device selection).  Peer access is not enabled: the
+// shards never read each other's memory.
 void init_cuda(GPU_INFO *gpu_info, int display) {
-  if (gpu_info->GPU_N > 1)
-    printf("GB300 build: %d GPUs requested; all instances run on GPU %d.\n", gpu_info->GPU_N,
-           gpu_info->whichGPUs[0]);
-  cudaGetDeviceProperties(&gpu_info->prop[0], gpu_info->whichGPUs[0]);
-  cudaSetDevice(gpu_info->whichGPUs[0]);
-  if (display == 1)
-    printf("> GPU%d = \"%15s\"\n", gpu_info->whichGPUs[0], gpu_info->prop[0].name);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess) ndev = 0;
+  for (int i = 0; i < gpu_info->GPU_N && i < 64; ++i) {
+    const int dev = gpu_info->whichGPUs[i];
+    if (dev < 0 || dev >= ndev) continue;   // refused by initialize_cufft
+    cudaGetDeviceProperties(&gpu_info->prop[i], dev);
+    cudaSetDevice(dev);
+    if (display == 1) printf("> GPU%d = \"%15s\"\n", i, gpu_info->prop[i].name);
+  }
+  if (gpu_info->GPU_N >= 1 && gpu_info->whichGPUs[0] >= 0 && gpu_info->whichGPUs[0] < ndev)
+    cudaSetDevice(gpu_info->whichGPUs[0]);
 }
 
 // init_cuda.cu:296-546
@@ -169,6 +184,26 @@ void initialize_cufft(GPU_INFO *gpu_info, CUFFT_INFO *c) {
   c->dy = c->ly / (double)Ny;
   c->dz = c->lz / (double)Nz;
 
+  // the reference's split (init_cuda.cu:312): Num_SCFT / GPU_N per device
+  const int n_gpu = gpu_info->GPU_N;
+  int per = 0, not_run = 0;
+  int st = scft_shard_plan(c->Num_SCFT, n_gpu, &per, &not_run);
+  if (st != SCFT_OK) {
+    report(nullptr, st, "initialize_cufft");
+    return;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess) ndev = 0;
+  for (int g = 0; g < n_gpu; ++g)
+    if (gpu_info->whichGPUs[g] < 0 || gpu_info->whichGPUs[g] >= ndev) {
+      fprintf(stderr, "initialize_cufft: -gpu%d=%d names no device (%d visible)\n", g,
+              gpu_info->whichGPUs[g], ndev);
+      return;
+    }
+  c->batch = per;
+  if (not_run)
+    printf("Instances %d to %d are not run: Num_SCFT %% GPU_N = %d (batch = Num_SCFT/GPU_N).\n",
+           n_gpu * per + 1, c->Num_SCFT, not_run);
   scft_params p = c->opts;   // ab.txt's optional keys (defaults when absent)
   if (p.ds0 == 0.0) scft_params_default(&p);   // not parsed by init_scft: the defaults
   p.nx = Nx; p.ny = Ny; p.nz = Nz;
@@ -176,17 +211,23 @@ void initialize_cufft(GPU_INFO *gpu_info, CUFFT_INFO *c) {
   p.hAB = c->hAB; p.fA = c->fA; p.ds0 = c->ds0;
   p.batch = c->batch;
   p.precision = c->precision;
-  p.device = gpu_info->whichGPUs ? gpu_info->whichGPUs[0] : 0;
-  int st = scft_create(&p, &c->gb300);
-  if (st != SCFT_OK) {
-    report(nullptr, st, "initialize_cufft");
-    c->gb300 = nullptr;
-    return;
+  for (int g = 0; g < n_gpu; ++g) {
+    p.device = gpu_info->whichGPUs[g];
+    st = scft_create(&p, &c->shard[g]);
+    if (st != SCFT_OK) {
+      report(nullptr, st, "initialize_cufft");
+      for (int k = 0; k < g; ++k) scft_destroy(c->shard[k]);
+      for (int k = 0; k < n_gpu; ++k) c->shard[k] = nullptr;
+      c->gb300 = nullptr;
+      return;
+    }
   }
+  c->n_shard = n_gpu;
+  c->gb300 = c->shard[0];
   printf("Wonderful We have successfully initialized GPU setting.\n");
   printf("Wonderful We have successfully initialized cufft setting.\n");
-  scft_ctx *ctx = c->gb300;
-  if (c->metrics[0]) scft_set_metrics_file(ctx, c->metrics);
+  if (c->metrics[0])
+    for (int g = 0; g < n_gpu; ++g) scft_set_metrics_file(c->shard[g], c->metrics);
   const long M = c->NxNyNz;
   // host arrays and wave-number tables (init_cuda.cu:380-428)
   c->wa = (double *)calloc(M * c->Num_SCFT, sizeof(double));
@@ -210,59 +251,77 @@ void initialize_cufft(GPU_INFO *gpu_info, CUFFT_INFO *c) {
     for (int j = 0; j < Ny; j++)
       for (int i = 0; i < Nx; i++)
         c->kxyzdz[(long)(k * Ny + j) * Nx + i] = exp(-c->ds0 * (c->kx[i] + c->ky[j] + c->kz[k]));
-  gpu_info->stream = (cudaStream_t *)malloc(sizeof(cudaStream_t));
-  gpu_info->stream[0] = ctx->st;
-  // initial fields (init_cuda.cu:435-456)
+  gpu_info->stream = (cudaStream_t *)malloc(sizeof(cudaStream_t) * n_gpu);
+  for (int g = 0; g < n_gpu; ++g) gpu_info->stream[g] = c->shard[g]->st;
+  // initial fields (init_cuda.cu:435-456): global instance g*batch + i of
+  // shard g reads phi_<g*batch+i+1>.dat
   if (c->intag == 1024) {
-    for (int i = 0; i < c->Num_SCFT; i++) {
-      char name[64];
-      snprintf(name, sizeof name, "phi_%d.dat", i + 1);
-      st = scft_read_phi_dat(ctx, name, i);
-      if (st != SCFT_OK) {
-        printf("Configration file %s did not exist, please check it in your directory.\n", name);
-        report(ctx, st, "initialize_cufft");
+    for (int g = 0; g < n_gpu; ++g) {
+      scft_ctx *ctx = use_shard(c, g);
+      for (int i = 0; i < per; i++) {
+        char name[64];
+        snprintf(name, sizeof name, "phi_%d.dat", g * per + i + 1);
+        st = scft_read_phi_dat(ctx, name, i);
+        if (st != SCFT_OK) {
+          printf("Configration file %s did not exist, please check it in your directory.\n",
+                 name);
+          report(ctx, st, "initialize_cufft");
+        }
       }
+      const long off = (long)g * per * M;
+      scft_get_field(ctx, SCFT_FIELD_WA, c->wa + off);
+      scft_get_field(ctx, SCFT_FIELD_WB, c->wb + off);
+      scft_get_field(ctx, SCFT_FIELD_PHA, c->pha + off);
+      scft_get_field(ctx, SCFT_FIELD_PHB, c->phb + off);
     }
-    scft_get_field(ctx, SCFT_FIELD_WA, c->wa);
-    scft_get_field(ctx, SCFT_FIELD_WB, c->wb);
-    scft_get_field(ctx, SCFT_FIELD_PHA, c->pha);
-    scft_get_field(ctx, SCFT_FIELD_PHB, c->phb);
   }
   printf("Wonderful We have successfully initialized CPU setting.\n");
-  c->wa_cu.assign(1, ctx->wa);
-  c->wb_cu.assign(1, ctx->wb);
-  c->pha_cu.assign(1, ctx->pha);
-  c->phb_cu.assign(1, ctx->phb);
-  c->qa_cu.assign(1, static_cast<double *>(ctx->q[SCFT_Q_A]));
-  c->qcb_cu.assign(1, static_cast<double *>(ctx->q[SCFT_Q_CB]));
-  c->qb_cu.assign(1, static_cast<double *>(ctx->q[SCFT_Q_B]));
-  c->qca_cu.assign(1, static_cast<double *>(ctx->q[SCFT_Q_CA]));
+  std::vector<double *> *mir[4] = {&c->qa_cu, &c->qcb_cu, &c->qb_cu, &c->qca_cu};
+  for (std::vector<double *> *v : {&c->wa_cu, &c->wb_cu, &c->pha_cu, &c->phb_cu, &c->qa_cu,
+                                   &c->qcb_cu, &c->qb_cu, &c->qca_cu, &c->qInt_cu, &c->wdz_cu,
+                                   &c->ql, &c->ffl})
+    v->assign(n_gpu, nullptr);
+  for (int g = 0; g < n_gpu; ++g) {
+    scft_ctx *ctx = c->shard[g];
+    c->wa_cu[g] = ctx->wa;
+    c->wb_cu[g] = ctx->wb;
+    c->pha_cu[g] = ctx->pha;
+    c->phb_cu[g] = ctx->phb;
+    for (int q = 0; q < 4; ++q) (*mir[q])[g] = static_cast<double *>(ctx->q[q]);
+    c->qInt_cu[g] = static_cast<double *>(ctx->qint);
+    c->wdz_cu[g] = static_cast<double *>(ctx->W[0]);
+    c->ql[g] = (double *)calloc(c->batch, sizeof(double));
+    c->ffl[g] = (double *)calloc(c->batch, sizeof(double));
+  }
   if (c->reference_layout) {
     // FP64 mirrors in the reference's g[b][r][s] layout (init_cuda.cu:522-526)
-    std::vector<double *> *mir[4] = {&c->qa_cu, &c->qcb_cu, &c->qb_cu, &c->qca_cu};
-    double *m[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<double *> m(4 * (size_t)n_gpu, nullptr);
     bool ok = true;
-    for (int q = 0; q < 4 && ok; ++q)
-      ok = cudaMalloc(&m[q], sizeof(double) * ctx->M * ctx->batch * (ctx->q_ns[q] + 1)) ==
-           cudaSuccess;
+    for (int g = 0; g < n_gpu && ok; ++g) {
+      scft_ctx *ctx = use_shard(c, g);
+      for (int q = 0; q < 4 && ok; ++q)
+        ok = cudaMalloc(&m[4 * g + q],
+                        sizeof(double) * ctx->M * ctx->batch * (ctx->q_ns[q] + 1)) == cudaSuccess;
+    }
     if (ok) {
-      for (int q = 0; q < 4; ++q) mir[q]->assign(1, m[q]);
+      for (int g = 0; g < n_gpu; ++g)
+        for (int q = 0; q < 4; ++q) (*mir[q])[g] = m[4 * g + q];
     } else {
       cudaGetLastError();
-      for (double *p : m) cudaFree(p);
+      for (int g = 0; g < n_gpu; ++g) {
+        use_shard(c, g);
+        for (int q = 0; q < 4; ++q) cudaFree(m[4 * g + q]);
+      }
       fprintf(stderr, "initialize_cufft: cannot allocate the reference-layout propagators; "
                       "keeping the contour-outer ones\n");
       c->reference_layout = 0;
     }
   }
-  c->qInt_cu.assign(1, static_cast<double *>(ctx->qint));
-  c->wdz_cu.assign(1, static_cast<double *>(ctx->W[0]));
-  c->ql.assign(1, (double *)calloc(c->batch, sizeof(double)));
-  c->ffl.assign(1, (double *)calloc(c->batch, sizeof(double)));
+  use_shard(c, 0);
   printf("Wonderful We have successfully initialized all the data.\n");
 }
 
-// cuda_scft.cu:14-59
+// cuda_scft.cu:14-59: every shard's instances (data[g] is shard g's array)
 void average_value(std::vector<double *> data, GPU_INFO *gpu_info, CUFFT_INFO *c) {
   (void)gpu_info;
   if (!c->gb300 || data.empty()) return;
@@ -271,8 +330,9 @@ void average_value(std::vector<double *> data, GPU_INFO *gpu_info, CUFFT_INFO *c
     fprintf(stderr, "average_value: pointer is not wa_cu or wb_cu\n");
     return;
   }
-  report(c->gb300, scft_average_value(c->gb300, f), "average_value");
-  scft_synchronize(c->gb300);
+  for (int g = 0; g < c->n_shard; ++g)
+    report(c->shard[g], scft_average_value(use_shard(c, g), f), "average_value");
+  for (int g = 0; g < c->n_shard; ++g) scft_synchronize(use_shard(c, g));
 }
 
 // cuda_scft.cu:435-563
@@ -285,65 +345,75 @@ void sovDifFft(GPU_INFO *gpu_info, CUFFT_INFO *c, std::vector<double *> g,
     fprintf(stderr, "sovDifFft: unknown propagator or field pointer\n");
     return;
   }
-  report(c->gb300, scft_sov_dif_fft(c->gb300, q, f, ns, sign), "sovDifFft");
-  scft_synchronize(c->gb300);
-  refresh_mirror(c, q);
+  for (int k = 0; k < c->n_shard; ++k)
+    report(c->shard[k], scft_sov_dif_fft(use_shard(c, k), q, f, ns, sign), "sovDifFft");
+  for (int k = 0; k < c->n_shard; ++k) {
+    scft_synchronize(use_shard(c, k));
+    refresh_mirror(c, k, q);
+  }
 }
 
-// cuda_scft.cu:61-138
+// cuda_scft.cu:61-138: queued on every shard before any is waited for
 void getConc(GPU_INFO *gpu_info, CUFFT_INFO *c) {
   (void)gpu_info;
   if (!c->gb300) return;
-  report(c->gb300, scft_get_conc(c->gb300), "getConc");
-  for (int q = 0; q < 4; ++q) refresh_mirror(c, q);
-  if (scft_get_Q(c->gb300, c->ql[0]) == SCFT_OK)
-    for (int i = 0; i < c->batch; ++i) c->ffl[0][i] = c->ds0 / c->ql[0][i];
+  for (int g = 0; g < c->n_shard; ++g)
+    report(c->shard[g], scft_get_conc(use_shard(c, g)), "getConc");
+  for (int g = 0; g < c->n_shard; ++g) {
+    scft_ctx *ctx = use_shard(c, g);
+    for (int q = 0; q < 4; ++q) refresh_mirror(c, g, q);
+    if (scft_get_Q(ctx, c->ql[g]) == SCFT_OK)
+      for (int i = 0; i < c->batch; ++i) c->ffl[g][i] = c->ds0 / c->ql[g][i];
+  }
 }
 
 // cuda_scft.cu:140-269: prints the progress lines and writes pha_<i>.dat in
-// the working directory, as the reference does.
+// the working directory, as the reference does, over every shard.
 double Free(GPU_INFO *gpu_info, CUFFT_INFO *c) {
   (void)gpu_info;
   if (!c->gb300) return 0;
-  report(c->gb300, scft_free(c->gb300, c->MaxIT, c->AverIt, "."), "Free");
-  scft_get_Q(c->gb300, c->ql[0]);
+  report(c->gb300, scft_free_shards(c->shard, c->n_shard, c->MaxIT, c->AverIt, "."), "Free");
+  for (int g = 0; g < c->n_shard; ++g) scft_get_Q(use_shard(c, g), c->ql[g]);
+  use_shard(c, 0);
   return 0;
 }
 
-// cuda_scft.cu:382-432
+// cuda_scft.cu:382-432.  The reference brackets Free with events on the
+// current device's default stream; Free synchronises every device before it
+// returns, so the host clock measures the same interval on any number of
+// shards.
 void fft_test(GPU_INFO *gpu_info, CUFFT_INFO *c) {
   if (!c->gb300) {
     printf("fft_test did not successfully detect run time\n");
     return;
   }
-  cudaEvent_t start, stop;
-  float msec = 0.f;
-  cudaEventCreate(&start);
-  cudaEventCreate(&stop);
-  cudaEventRecord(start, c->gb300->st);
+  const auto t0 = std::chrono::steady_clock::now();
   Free(gpu_info, c);
-  cudaEventRecord(stop, c->gb300->st);
-  cudaEventSynchronize(stop);
-  if (cudaEventElapsedTime(&msec, start, stop) != cudaSuccess)
-    printf("fft_test did not successfully detect run time\n");
+  const double msec =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   printf("time=%0.10f\n", msec);
-  cudaEventDestroy(start);
-  cudaEventDestroy(stop);
 }
 
 // init_cuda.cu:551-628
 void finalize_cufft(GPU_INFO *gpu_info, CUFFT_INFO *c) {
-  if (c->reference_layout && c->gb300) {
-    std::vector<double *> *mir[4] = {&c->qa_cu, &c->qcb_cu, &c->qb_cu, &c->qca_cu};
-    for (auto *m : mir)
-      if (!m->empty()) cudaFree((*m)[0]);
+  std::vector<double *> *mir[4] = {&c->qa_cu, &c->qcb_cu, &c->qb_cu, &c->qca_cu};
+  for (int g = 0; g < c->n_shard; ++g) {
+    if (!c->shard[g]) continue;
+    use_shard(c, g);
+    if (c->reference_layout)
+      for (auto *m : mir)
+        if ((int)m->size() > g) cudaFree((*m)[g]);
+    scft_destroy(c->shard[g]);
+    c->shard[g] = nullptr;
   }
-  if (c->gb300) scft_destroy(c->gb300);
+  c->n_shard = 0;
   c->gb300 = nullptr;
   free(c->wa); free(c->wb); free(c->pha); free(c->phb);
   free(c->kx); free(c->ky); free(c->kz); free(c->kxyzdz);
-  if (!c->ql.empty()) free(c->ql[0]);
-  if (!c->ffl.empty()) free(c->ffl[0]);
+  for (double *q : c->ql) free(q);
+  for (double *f : c->ffl) free(f);
+  c->ql.clear();
+  c->ffl.clear();
   free(gpu_info->stream);
   free(gpu_info->whichGPUs);
   gpu_info->stream = nullptr;

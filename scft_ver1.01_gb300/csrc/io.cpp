@@ -338,37 +338,65 @@ int scft_load_checkpoint(scft_ctx *ctx, const char *path) {
   if (!ctx || !path) return SCFT_ERR_INVALID_ARG;
   FILE *fp = fopen(path, "rb");
   if (!fp) return scft_fail(ctx, SCFT_ERR_IO, std::string("cannot open ") + path);
+  auto io_fail = [&](int st, const std::string &m) {
+    fclose(fp);
+    return scft_fail(ctx, st, m);
+  };
   CkptHeader h;
-  if (fread(&h, sizeof h, 1, fp) != 1 || memcmp(h.magic, "SCFTCKP1", 8) != 0 || h.version != 1) {
-    fclose(fp);
-    return scft_fail(ctx, SCFT_ERR_IO, std::string("not a checkpoint file: ") + path);
-  }
+  if (fread(&h, sizeof h, 1, fp) != 1 || memcmp(h.magic, "SCFTCKP1", 8) != 0 || h.version != 1)
+    return io_fail(SCFT_ERR_IO, std::string("not a checkpoint file: ") + path);
   const scft_params &p = ctx->p;
-  if (h.nx != p.nx || h.ny != p.ny || h.nz != p.nz || h.batch != ctx->batch) {
-    fclose(fp);
-    return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "checkpoint grid or batch differs from the context");
+  if (h.nx != p.nx || h.ny != p.ny || h.nz != p.nz || h.batch != ctx->batch)
+    return io_fail(SCFT_ERR_INVALID_ARG, "checkpoint grid or batch differs from the context");
+  // The whole file is checked against the size its header implies before
+  // anything reaches the device, so a short or padded file leaves the
+  // context's fields and history as they were.
+  const long long BM = ctx->M * ctx->batch;
+  const long long fields_bytes = (4 * BM + 4LL * ctx->batch) * (long long)sizeof(double);
+  const long long off_m1 = (long long)sizeof h + fields_bytes;
+  if (fseek(fp, 0, SEEK_END) != 0) return io_fail(SCFT_ERR_IO, "checkpoint seek failed");
+  const long long size = ftell(fp);
+  int32_t m1 = 0;
+  long long expect = off_m1;
+  if (h.has_history) {
+    if (size < off_m1 + (long long)sizeof m1 || fseek(fp, off_m1, SEEK_SET) != 0 ||
+        fread(&m1, sizeof m1, 1, fp) != 1)
+      return io_fail(SCFT_ERR_IO, "checkpoint file is short");
+    if (m1 < 2 || m1 > 64) return io_fail(SCFT_ERR_IO, "checkpoint history length is corrupt");
+    expect += (long long)sizeof m1 +
+              ((long long)m1 * 2 * 2 * BM + (long long)ctx->batch * m1 * m1) *
+                  (long long)sizeof(double);
   }
+  if (size != expect)
+    return io_fail(SCFT_ERR_IO, size < expect ? "checkpoint file is short"
+                                              : "checkpoint file has trailing bytes");
+  // fields and residual norms through one host buffer, then to the device
+  std::vector<double> host((size_t)(4 * BM + 4LL * ctx->batch));
+  if (fseek(fp, (long)sizeof h, SEEK_SET) != 0 ||
+      fread(host.data(), sizeof(double), host.size(), fp) != host.size())
+    return io_fail(SCFT_ERR_IO, "checkpoint read failed");
   cudaSetDevice(ctx->p.device);
   cudaError_t e = cudaStreamSynchronize(ctx->st);
-  if (e != cudaSuccess) {
-    fclose(fp);
-    return scft_fail(ctx, SCFT_ERR_CUDA, cudaGetErrorString(e));
-  }
-  const long long BM = ctx->M * ctx->batch;
+  if (e != cudaSuccess) return io_fail(SCFT_ERR_CUDA, cudaGetErrorString(e));
   double *fields[4] = {ctx->wa, ctx->wb, ctx->pha, ctx->phb};
-  int rc = SCFT_OK;
-  for (int k = 0; k < 4 && rc == SCFT_OK; ++k) rc = file_to_dev(ctx, fp, fields[k], BM);
-  if (rc == SCFT_OK) rc = file_to_dev(ctx, fp, ctx->res, 4LL * ctx->batch);
+  for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+    e = cudaMemcpy(fields[k], host.data() + k * BM, sizeof(double) * BM, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(ctx->res, host.data() + 4 * BM, sizeof(double) * 4 * ctx->batch,
+                   cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return io_fail(SCFT_ERR_CUDA, cudaGetErrorString(e));
+  std::vector<double>().swap(host);
+  // the history restarts unless the file's ring belongs to this operator; a
+  // ring only counts once it is fully copied (and_count stays 0 until then)
   ctx->and_count = 0;
   ctx->have_conc = false;   // the stored propagators belong to other fields
-  if (rc == SCFT_OK && h.has_history) {
-    int32_t m1 = 0;
+  int rc = SCFT_OK;
+  if (h.has_history) {
     const bool same = history_kept(ctx) && h.precision == p.precision &&
                       h.mixing == p.mixing && h.history == p.anderson_history &&
                       h.lx == p.lx && h.ly == p.ly && h.lz == p.lz && h.hAB == p.hAB &&
                       h.fA == p.fA && h.ds0 == p.ds0;
-    if (fread(&m1, sizeof m1, 1, fp) != 1) rc = scft_fail(ctx, SCFT_ERR_IO, "checkpoint file is short");
-    if (rc == SCFT_OK && same && m1 == ctx->m1) {
+    if (same && m1 == ctx->m1 && fseek(fp, (long)(off_m1 + (long long)sizeof m1), SEEK_SET) == 0) {
       for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = file_to_dev(ctx, fp, ctx->hist_w[j], 2 * BM);
       for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = file_to_dev(ctx, fp, ctx->hist_d[j], 2 * BM);
       if (rc == SCFT_OK) rc = file_to_dev(ctx, fp, ctx->gram, (long long)ctx->batch * m1 * m1);

@@ -3,30 +3,36 @@
 //
 // Who needs it: callers that cannot call cudaMalloc at the point where they
 // advance a propagator.  For example, a host framework that owns all device
-// memory through its own pool and forbids raw allocations in plug-ins; code
-// that runs while a stream is being captured into a CUDA graph (cudaMalloc is
-// not allowed during capture); or latency-critical loops where cudaMalloc's
-// implicit device synchronisation is unacceptable.  They pass their own input,
+// memory through its own pool and forbids raw allocations in plug-ins, or a
+// latency-critical loop where cudaMalloc's implicit device synchronisation is
+// unacceptable.  They pass their own input,
 // Boltzmann factor and output buffers; everything else the step needs (the
 // two intermediates between the per-axis passes and the per-axis FFT tables)
 // lives in the file-scope scratch array below.
 //
 // Limits and sharing:
 //  - batch * Nx*Ny*Nz must not exceed kNoAllocMaxPoints (2^21, e.g. one 128^3
-//    grid or eight 64^3 grids); axes up to 4096 points.  Larger requests are
-//    rejected with SCFT_ERR_INVALID_ARG.
+//    grid or eight 64^3 grids), batch must not exceed 65535 (the launch grid's
+//    z limit); axes up to 4096 points.  Larger requests are rejected with
+//    SCFT_ERR_INVALID_ARG before anything is enqueued.
 //  - The array (2 * 2^21 floats + tables, about 16.2 MB) is held by every GPU
 //    that loads this library, until the process exits.
 //  - Every call shares the one array: two calls whose work overlaps on the GPU
 //    (different streams, or different host threads) race on it.  Serialise
 //    them on one stream.
 //  - The first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) and sets kernel attributes; make that first call
-//    before any stream capture on that device.
+//    (cudaGetSymbolAddress) and sets kernel attributes, once per device under
+//    a lock (host threads may race to it); make that first call before any
+//    stream capture on that device.
+//  - A failure is this call's own: each launch's status is read from its own
+//    cudaLaunchKernelEx, never from the thread's last-error state, so an
+//    earlier unrelated runtime error does not fail a valid call.
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
+#include <mutex>
 #include <string>
 
 #include "ctx.h"
@@ -43,7 +49,9 @@ constexpr int kMaxDevices = 64;
 // intermediate is fully written by one pass before the next pass reads it.
 static __device__ __align__(256) float g_noalloc_scratch[2 * kNoAllocMaxPoints + kTableFloats];
 
-float *g_scratch_dev[kMaxDevices] = {nullptr};   // device address of the array, per device
+// device address of the array, per device; set once under g_setup_mu
+std::atomic<float *> g_scratch_dev[kMaxDevices];
+std::mutex g_setup_mu;
 thread_local std::string g_noalloc_err = "no error";   // per host thread
 
 int fail(int st, const std::string &m) {
@@ -86,6 +94,9 @@ extern "C" int scft_split_step_noalloc(int nx, int ny, int nz, double lx, double
     return fail(SCFT_ERR_INVALID_ARG, "q_in, W and q_out must be 16-byte aligned");
   if (batch < 1 || !(lx > 0 && ly > 0 && lz > 0 && ds0 > 0))
     return fail(SCFT_ERR_INVALID_ARG, "bad batch, box or ds0");
+  if (batch > 65535)
+    return fail(SCFT_ERR_INVALID_ARG, "batch " + std::to_string(batch) +
+                                          " exceeds the launch limit of 65535 instances");
   if (!scft_grid_supported(nx, ny, nz) || nx > kNoAllocMaxAxis || ny > kNoAllocMaxAxis ||
       nz > kNoAllocMaxAxis)
     return fail(SCFT_ERR_UNSUPPORTED, "grid not supported by the kernels");
@@ -99,18 +110,24 @@ extern "C" int scft_split_step_noalloc(int nx, int ny, int nz, double lx, double
     return fail(SCFT_ERR_NO_DEVICE, "no current CUDA device");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
 
-  // once per device, with that device current
-  if (!g_scratch_dev[dev]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess)
-      return fail(SCFT_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    if (scft::line_filter_prepare() != cudaSuccess || scft::fast_line_prepare() != cudaSuccess)
-      return fail(SCFT_ERR_CUDA, "kernel attribute set-up failed");
-    g_scratch_dev[dev] = static_cast<float *>(p);
+  // once per device, with that device current (host threads may race here)
+  float *scratch = g_scratch_dev[dev].load(std::memory_order_acquire);
+  if (!scratch) {
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    scratch = g_scratch_dev[dev].load(std::memory_order_relaxed);
+    if (!scratch) {
+      void *p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess)
+        return fail(SCFT_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      if (scft::line_filter_prepare() != cudaSuccess || scft::fast_line_prepare() != cudaSuccess)
+        return fail(SCFT_ERR_CUDA, "kernel attribute set-up failed");
+      scratch = static_cast<float *>(p);
+      g_scratch_dev[dev].store(scratch, std::memory_order_release);
+    }
   }
-  float *tmp[2] = {g_scratch_dev[dev], g_scratch_dev[dev] + kNoAllocMaxPoints};
-  float *tables = g_scratch_dev[dev] + 2 * kNoAllocMaxPoints;
+  float *tmp[2] = {scratch, scratch + kNoAllocMaxPoints};
+  float *tables = scratch + 2 * kNoAllocMaxPoints;
 
   // per-axis passes, as scft_create builds them (length-1 axes fold into the first)
   const int dims[3] = {nx, ny, nz};
@@ -151,9 +168,20 @@ extern "C" int scft_split_step_noalloc(int nx, int ny, int nz, double lx, double
     float *gain = tw + 2 * kNoAllocMaxAxis;
     ap.twiddle = tw;
     ap.gain = gain;
-    k_noalloc_tables<<<(n + 255) / 256, 256, 0, st>>>(tw, gain, n, lens[a], ds0,
-                                                      i == 0 ? scale : 1.0);
-    cudaError_t e = cudaGetLastError();
+    // The pass kernels read their tables before their dependency wait
+    // (griddepcontrol.wait), overlapping the previous kernel's tail.  That is
+    // safe here because every table kernel is enqueued, without the
+    // programmatic-launch attribute, before the first pass: a pass can only
+    // overlap the last table kernel or an earlier pass, and the first pass
+    // reads the first axis's tables, which an earlier table kernel wrote (with
+    // one axis, the first pass is the generic kernel, which waits first).
+    // Keep the table launches ahead of every pass.
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((n + 255) / 256);
+    cfg.blockDim = dim3(256);
+    cfg.stream = st;
+    const double len = lens[a], sc = i == 0 ? scale : 1.0;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_noalloc_tables, tw, gain, n, len, ds0, sc);
     if (e != cudaSuccess) return fail(SCFT_ERR_CUDA, cudaGetErrorString(e));
   }
   // the split step: W . D_z D_y D_x (W . q_in), one pass per axis

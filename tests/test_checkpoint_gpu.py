@@ -93,14 +93,48 @@ def test_checkpoint_errors(pkg, tmp_path):
         with pytest.raises(pkg.ScftError) as e:
             b.load_checkpoint(tmp_path / "missing.ckpt")
         assert e.value.status == pkg.ERR_IO
-    # a truncated file: the fields are short
+    # a truncated file (the fields are short) or one with trailing bytes: an
+    # error, and the context's fields are unchanged (the file is checked
+    # whole before anything reaches the device)
     data = path.read_bytes()
     short = tmp_path / "short.ckpt"
+    long_ = tmp_path / "long.ckpt"
     short.write_bytes(data[: len(data) // 2])
+    long_.write_bytes(data + b"\0" * 8)
     with pkg.Context(**ctx_kw(pkg, "fp64", "simple")) as c:
+        w0 = [x + 0.25 for x in start_fields()]
+        c.set_w(*w0)
+        for f in (short, long_):
+            with pytest.raises(pkg.ScftError) as e:
+                c.load_checkpoint(f)
+            assert e.value.status == pkg.ERR_IO
+            assert np.array_equal(c.wa, w0[0]) and np.array_equal(c.wb, w0[1])
+
+
+def test_truncated_history_leaves_the_context_unchanged(pkg, tmp_path):
+    """A checkpoint cut inside its Anderson history: the load fails before
+    any field or history slot is touched, and the run continues exactly as
+    it would have without the attempt."""
+    wa, wb = start_fields()
+    path = tmp_path / "run.ckpt"
+    kw = ctx_kw(pkg, "fp64", "anderson")
+    with pkg.Context(**kw) as a:
+        a.set_w(wa, wb)
+        a.iterate(7)
+        a.save_checkpoint(path)
+    data = path.read_bytes()
+    cut = tmp_path / "cut.ckpt"
+    cut.write_bytes(data[: len(data) - 1000])
+    with pkg.Context(**kw) as b, pkg.Context(**kw) as ref:
+        for c in (b, ref):
+            c.set_w(wa + 0.1, wb - 0.1)
+            c.iterate(4)
         with pytest.raises(pkg.ScftError) as e:
-            c.load_checkpoint(short)
+            b.load_checkpoint(cut)
         assert e.value.status == pkg.ERR_IO
+        b.iterate(3)
+        ref.iterate(3)
+        assert np.array_equal(b.wa, ref.wa) and np.array_equal(b.wb, ref.wb)
 
 
 def test_free_writes_json_lines(pkg, tmp_path, capfd):

@@ -153,3 +153,112 @@ def test_struct_api_reference_layout(pkg, orc, tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     line = [l for l in r.stdout.splitlines() if l.startswith("layout_maxdiff=")][0]
     assert line == "layout_maxdiff=0 reference_layout=1", line
+
+
+REF_MAIN_STAGED = os.path.join(ROOT, "oracle", "_ref", "ref_main.cpp")
+
+
+def build_reference_main(tmp_path):
+    """The reference's main.cpp (main.cpp:20-41), unchanged, compiled against
+    include/compat/ and linked with this library.  oracle/Makefile stages it
+    byte for byte beside the reference-kernel cubin; -I- keeps its quoted
+    includes off the directory it sits in."""
+    import shutil
+    if not os.path.exists(REF_MAIN_STAGED):
+        pytest.skip("reference driver source not staged (oracle/_ref/ref_main.cpp)")
+    pkgdir = os.path.join(ROOT, "scft_ver1.01_gb300")
+    exe = str(tmp_path / "ref_driver")
+    r = subprocess.run([shutil.which("g++"), "-std=c++17", "-iquote",
+                        os.path.join(ROOT, "include", "compat"), "-I-",
+                        "-I" + os.path.join(ROOT, "include", "compat"),
+                        "-I" + os.path.join(ROOT, "include"), "-I/usr/local/cuda/include",
+                        REF_MAIN_STAGED, "-L" + pkgdir, "-lscft_gb300",
+                        "-Wl,-rpath=" + pkgdir, "-o", exe],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_reference_main_runs_unchanged(pkg, orc, tmp_path):
+    """The reference's own driver gives the same progress lines and pha files
+    as this library's driver, and the oracle's Free loop."""
+    exe = build_reference_main(tmp_path)
+    from scft_gb300 import fields
+    p = orc.Params(nx=16, ny=16, nz=8, lx=4.0, ly=4.0, lz=2.0, hAB=20.0, fA=0.5, ds0=0.01,
+                   batch=2)
+    wa, wb = fields.lamellar(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 20.0, seed=8, batch=2)
+    out = {}
+    for name, prog in (("ref", exe), ("ours", DRIVER)):
+        d = tmp_path / name
+        d.mkdir()
+        write_case(orc, str(d), p, wa, wb)
+        r = subprocess.run([prog, "-step=100"], cwd=str(d), capture_output=True, text=True,
+                           timeout=600)
+        assert r.returncode == 0, r.stdout + r.stderr
+        out[name] = ([l for l in r.stdout.splitlines() if l.startswith("GPU ")],
+                     [open(d / ("pha_%d.dat" % (i + 1))).read() for i in range(2)])
+        assert any(l.startswith("time=") for l in r.stdout.splitlines())
+    assert len(out["ref"][0]) == 20
+    assert out["ref"] == out["ours"]                # identical lines and files
+    d = str(tmp_path / "ref")
+    wa0 = np.stack([orc.read_phi_dat(os.path.join(d, "phi_%d.dat" % (i + 1)), p.M)[2]
+                    for i in range(2)]).reshape((2,) + p.shape)
+    wb0 = np.stack([orc.read_phi_dat(os.path.join(d, "phi_%d.dat" % (i + 1)), p.M)[3]
+                    for i in range(2)]).reshape((2,) + p.shape)
+    ref = orc.free_loop(wa0, wb0, p, 100)
+    for l, row in zip(out["ref"][0], ref.log):
+        it, b, F, fab, fw, fs, inc = row
+        assert l.startswith("GPU 0 batch %d: %5d :" % (b, it))
+        vals = [float(v) for v in l.split(":")[2].split(",")]
+        np.testing.assert_allclose(vals[:4], [F, fab, fw, fs], rtol=1e-7, atol=1e-9)
+    pa = orc.read_phi_dat(os.path.join(d, "pha_1.dat"), p.M)[0]
+    np.testing.assert_allclose(pa, ref.pha[0].ravel(), rtol=1e-4, atol=1e-5)
+
+
+def test_driver_splits_instances_over_devices(pkg, orc, tmp_path):
+    """-GPU_N=2 with both shards listed on device 0 (the only one a test box
+    has): three instances split as the reference does (init_cuda.cu:312,
+    batch = 3/2 = 1 per device, the third not run); the progress lines
+    number devices and instances as the reference's Free prints them
+    (cuda_scft.cu:221) and pha_<g*batch+i+1>.dat holds each shard's instance."""
+    from scft_gb300 import fields
+    p = orc.Params(nx=16, ny=16, nz=8, lx=4.0, ly=4.0, lz=2.0, hAB=20.0, fA=0.5, ds0=0.01,
+                   batch=3)
+    wa, wb = fields.lamellar(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 20.0, seed=9, batch=3)
+    d = str(tmp_path)
+    write_case(orc, d, p, wa, wb)
+    r = subprocess.run([DRIVER, "-step=100", "-GPU_N=2", "-gpu0=0", "-gpu1=0"], cwd=d,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Instances 3 to 3 are not run" in r.stdout
+    lines = [l for l in r.stdout.splitlines() if l.startswith("GPU ")]
+    assert len(lines) == 20                      # every 10 iterations x 2 shards x 1 instance
+    assert lines[0].startswith("GPU 0 batch 0:") and lines[1].startswith("GPU 1 batch 0:")
+    assert not os.path.exists(os.path.join(d, "pha_3.dat"))
+    p1 = orc.Params(nx=16, ny=16, nz=8, lx=4.0, ly=4.0, lz=2.0, hAB=20.0, fA=0.5, ds0=0.01,
+                    batch=1)
+    for g in range(2):
+        fn = os.path.join(d, "phi_%d.dat" % (g + 1))
+        w = orc.read_phi_dat(fn, p.M)
+        ref = orc.free_loop(w[2].reshape((1,) + p.shape), w[3].reshape((1,) + p.shape), p1, 100)
+        mine = [l for l in lines if l.startswith("GPU %d batch 0:" % g)]
+        for l, row in zip(mine, ref.log):
+            vals = [float(v) for v in l.split(":")[2].split(",")]
+            np.testing.assert_allclose(vals[:4], row[2:6], rtol=1e-7, atol=1e-9)
+        pa = orc.read_phi_dat(os.path.join(d, "pha_%d.dat" % (g + 1)), p.M)[0]
+        np.testing.assert_allclose(pa, ref.pha[0].ravel(), rtol=1e-4, atol=1e-5)
+
+
+def test_driver_refuses_a_missing_device(pkg, orc, tmp_path):
+    import torch
+    from scft_gb300 import fields
+    p = orc.Params(nx=16, ny=16, nz=8, lx=4.0, ly=4.0, lz=2.0, hAB=20.0, fA=0.5, ds0=0.01,
+                   batch=2)
+    wa, wb = fields.lamellar(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 20.0, seed=9, batch=2)
+    d = str(tmp_path)
+    write_case(orc, d, p, wa, wb)
+    missing = torch.cuda.device_count()
+    r = subprocess.run([DRIVER, "-step=10", "-GPU_N=2", "-gpu1=%d" % missing], cwd=d,
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0
+    assert "-gpu1=%d names no device" % missing in r.stderr

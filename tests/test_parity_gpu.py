@@ -62,6 +62,38 @@ def test_march_parity(pkg, orc, g, prec):
             assert rel(ctx.get_q(pkg.Q_CB, s), ref_cb[:, s]) < TOL[prec], s
 
 
+# Long column lines: the fused z kernels k_zz<T, 128, 8> (the benchmark grid's
+# z pass, in FP32, FP64 and double-float) and k_zz<float, 256, 16> (the 256^3
+# workload's z pass), compared with the oracle slice by slice.
+LONG_Z = [
+    ((64, 64, 128, 3.8, 3.8, 3.8), (0, 1, 2)),
+    ((128, 128, 128, 3.8, 3.8, 3.8), (0, 1, 2)),
+    ((64, 32, 256, 3.0, 2.0, 8.0), (1,)),
+]
+
+
+@pytest.mark.parametrize("g,prec", [(g, p) for g, ps in LONG_Z for p in ps],
+                         ids=[f"{g[0]}x{g[1]}x{g[2]}-{ {0: 'fp64', 1: 'fp32', 2: 'df'}[p]}"
+                              for g, ps in LONG_Z for p in ps])
+def test_march_parity_long_columns(pkg, orc, g, prec):
+    """sovDifFft (cuda_scft.cu:435-563) with every contour slice compared."""
+    from scft_gb300 import fields
+    kw = dict(hAB=18.0, fA=0.36, ds0=0.02)
+    p = oparams(orc, g, batch=1, **kw)
+    wa, _ = fields.gyroid(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, 18.0, seed=2, batch=1)
+    tol = {0: 1e-11, 1: 2e-5, 2: 1e-10}[prec]
+    with make_ctx(pkg, g, prec, batch=1, **kw) as ctx:
+        ctx.set_w(wa, -wa)
+        ctx.set_qint(-1)
+        ctx.sov_dif_fft(pkg.Q_A, pkg.FIELD_WA, ctx.NsA, +1)
+        sched, _ = ctx.schedule()
+        ref = orc.sov_dif_fft(np.ones_like(wa), wa, p.NsA, +1, p)
+        for s_ in range(p.NsA + 1):
+            assert rel(ctx.get_q(pkg.Q_A, s_), ref[:, s_]) < tol, s_
+    # the fused step pairs (and with them the long z kernels) ran
+    assert not sched & pkg.FLAG_NO_FUSED_STEPS
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("g", GRIDS[:5] + GRIDS[7:9])
 def test_get_conc_parity(pkg, orc, g, prec):

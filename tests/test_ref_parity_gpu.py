@@ -21,6 +21,9 @@ def ref_mod():
 
 
 CFG = [
+    # the benchmark workload: 128^3 double gyroid, f=0.36, chiN=18, box 3.8,
+    # Ns=200 (NsA=72, dNsB=128); its z lines run k_zz<*, 128, 8>
+    ((128, 128, 128), (3.8, 3.8, 3.8), 18.0, 0.36, 0.005, "gyroid"),
     # 64^3 double gyroid, f=0.36, chiN=18, box 3.8, Ns=200
     ((64, 64, 64), (3.8, 3.8, 3.8), 18.0, 0.36, 0.005, "gyroid"),
     # 128x128x64 hexagonal cylinders, f=0.3, chiN=25, Lx=4.2, Ly=Lx*sqrt(3), Lz=2.0, Ns=200
@@ -30,9 +33,18 @@ CFG = [
 ]
 
 
-@pytest.mark.parametrize("cfg", CFG, ids=["gyroid64", "hex128x128x64", "lam32"])
-@pytest.mark.parametrize("prec,tol", [(0, 1e-11), (1, 2e-5)])
+IDS = ["gyroid128", "gyroid64", "hex128x128x64", "lam32"]
+# double-float needs register-resident passes on every axis (not 32^3)
+PRECS = [(0, 1e-11), (1, 2e-5), (2, 1e-10)]
+CASES = [(c, p, t) for c in CFG for p, t in PRECS if not (p == 2 and c[0][0] == 32)]
+CASE_IDS = [f"{IDS[CFG.index(c)]}-{ {0: 'fp64', 1: 'fp32', 2: 'df'}[p]}" for c, p, _ in CASES]
+
+
+@pytest.mark.parametrize("cfg,prec,tol", CASES, ids=CASE_IDS)
 def test_get_conc_vs_reference_kernels(pkg, ref_mod, cfg, prec, tol):
+    """getConc (cuda_scft.cu:61-138) of the CUDA path against the reference's
+    own kernels and cuFFT FP64 on the same fields: phi, Q and the boundary
+    slices of the four propagators."""
     from scft_gb300 import fields as fl
     grid, box, chiN, fA, ds0, init = cfg
     gen = getattr(fl, init)
@@ -41,6 +53,10 @@ def test_get_conc_vs_reference_kernels(pkg, ref_mod, cfg, prec, tol):
     r.set_w(wa, wb)
     r.get_conc()
     ref_pha, ref_phb, ref_Q = r.get_field(2), r.get_field(3), r.Q()
+    # propagator slices: qA at the A/B junction, qB's end (Q's slice) and
+    # q+A at s = 0 (the last slice of the second backward march)
+    ref_q = {(0, r.NsA): r.get_q(0, r.NsA), (2, r.dNsB): r.get_q(2, r.dNsB),
+             (3, 0): r.get_q(3, 0)}
     r.close()
     nx, ny, nz = grid
     lx, ly, lz = box
@@ -51,6 +67,8 @@ def test_get_conc_vs_reference_kernels(pkg, ref_mod, cfg, prec, tol):
         assert rel(ctx.pha, ref_pha) < tol
         assert rel(ctx.phb, ref_phb) < tol
         assert abs(ctx.Q()[0] / ref_Q[0] - 1) < tol
+        for (q, s_), v in ref_q.items():
+            assert rel(ctx.get_q(q, s_), v) < tol, (q, s_)
 
 
 def test_loop_vs_reference_kernels(pkg, ref_mod):
