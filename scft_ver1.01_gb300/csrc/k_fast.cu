@@ -23,11 +23,14 @@
 
 #include "common.cuh"
 #include "fft_reg.cuh"
+#include "filter_core.cuh"
 #include "kernels.h"
 
 namespace scft {
 
 namespace {
+
+using namespace fcore;
 
 // Shared memory of k_fast_line before its tables: the exchange buffer
 // (N x 32 complex), or the 64-row staging tile (pitch N+1) of the x pass,
@@ -38,126 +41,6 @@ template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_
              : (((size_t)64 * (N + 1) * sizeof(T) + 15) / 16) * 16;
 }
 
-// ------------------------------------------------------------------------
-// The four-step filter core (FP32 or FP64 complex C, real T): v[j] holds
-// element p + P*j of complex column `lane` on entry and the filtered values
-// on exit.  `after_first_sync` runs once every warp has written its stage-1
-// exchange slots (so every warp has finished reading its inputs).
-// bar_id 0 synchronises the whole CTA; bar_id > 0 only the P warps of one
-// warp group (named barrier bar_id), so several groups can filter
-// independent line sets in one CTA.
-__device__ __forceinline__ void group_sync(int bar_id, int nthreads) {
-  if (bar_id == 0) __syncthreads();
-  else asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(nthreads) : "memory");
-}
-
-template <int N, int P, typename C, typename T, typename F>
-__device__ __forceinline__ void four_step(C (&v)[N / P], C *ex, const C *tw, const T *gain, int p,
-                                          int lane, int bar_id, F &&after_first_sync) {
-  constexpr int R1 = N / P;
-  reg::dft<R1, false>(v);
-  reg::static_for<0, R1>([&](auto k_) {
-    constexpr int k1 = decltype(k_)::value;
-    if (k1 > 0) v[k1] = cmul(v[k1], tw[p * k1]);
-    ex[(k1 * P + p) * 32 + lane] = v[k1];
-  });
-  group_sync(bar_id, P * 32);
-  after_first_sync();
-  for (int k1 = p; k1 < R1; k1 += P) {
-    C u[P];
-    reg::static_for<0, P>([&](auto q_) {
-      constexpr int q = decltype(q_)::value;
-      u[q] = ex[(k1 * P + q) * 32 + lane];
-    });
-    reg::dft<P, false>(u);
-    reg::static_for<0, P>([&](auto k2_) {
-      constexpr int k2 = decltype(k2_)::value;
-      const T g = gain[k1 + R1 * k2];
-      u[k2].x *= g;
-      u[k2].y *= g;
-    });
-    reg::dft<P, true>(u);
-    reg::static_for<0, P>([&](auto q_) {
-      constexpr int q = decltype(q_)::value;
-      if (q > 0) u[q] = cmul(u[q], cconj(tw[q * k1]));
-      ex[(k1 * P + q) * 32 + lane] = u[q];
-    });
-  }
-  group_sync(bar_id, P * 32);
-  reg::static_for<0, R1>([&](auto k_) {
-    constexpr int k1 = decltype(k_)::value;
-    v[k1] = ex[(k1 * P + p) * 32 + lane];
-  });
-  reg::dft<R1, true>(v);
-  group_sync(bar_id, P * 32);   // the exchange buffer is free again
-}
-
-template <int R, typename C> __device__ __forceinline__ void conj_all(C (&a)[R]) {
-#pragma unroll
-  for (int i = 0; i < R; ++i) a[i].y = -a[i].y;
-}
-
-// The same filter with less code, for the double-float type: each pair
-// operation is 7-11 FP32 instructions, and the fully unrolled four_step (four
-// codelets, called twice per fused kernel) overflows the instruction cache
-// (measured: instruction-fetch stalls dominate).  Here the inverse DFTs are
-// conj(DFT(conj(x))) and the forward and inverse halves run as rolled loops,
-// so each codelet is emitted once.  Synchronises the whole CTA (bar 0).
-template <int N, int P, typename C, typename T>
-__device__ __forceinline__ void four_step_compact(C (&v)[N / P], C *ex, const C *tw,
-                                                  const T *gain, int p, int lane) {
-  constexpr int R1 = N / P;
-#pragma unroll 1
-  for (int phase = 0; phase < 2; ++phase) {
-    if (phase == 1) {
-      reg::static_for<0, R1>([&](auto k_) {
-        constexpr int k1 = decltype(k_)::value;
-        v[k1] = ex[(k1 * P + p) * 32 + lane];
-      });
-      conj_all(v);
-    }
-    reg::dft<R1, false>(v);
-    if (phase == 1) {
-      conj_all(v);
-      break;
-    }
-    reg::static_for<0, R1>([&](auto k_) {
-      constexpr int k1 = decltype(k_)::value;
-      if (k1 > 0) v[k1] = cmul(v[k1], tw[p * k1]);
-      ex[(k1 * P + p) * 32 + lane] = v[k1];
-    });
-    __syncthreads();
-    for (int k1 = p; k1 < R1; k1 += P) {
-      C u[P];
-      reg::static_for<0, P>([&](auto q_) {
-        constexpr int q = decltype(q_)::value;
-        u[q] = ex[(k1 * P + q) * 32 + lane];
-      });
-#pragma unroll 1
-      for (int dir = 0; dir < 2; ++dir) {
-        reg::dft<P, false>(u);
-        if (dir == 1) break;
-        reg::static_for<0, P>([&](auto k2_) {
-          constexpr int k2 = decltype(k2_)::value;
-          const T g = gain[k1 + R1 * k2];
-          u[k2].x *= g;
-          u[k2].y *= g;
-        });
-        conj_all(u);
-      }
-      conj_all(u);
-      reg::static_for<0, P>([&](auto q_) {
-        constexpr int q = decltype(q_)::value;
-        if (q > 0) u[q] = cmul(u[q], cconj(tw[q * k1]));
-        ex[(k1 * P + q) * 32 + lane] = u[q];
-      });
-    }
-    __syncthreads();
-  }
-  __syncthreads();   // the exchange buffer is free again
-}
-
-template <typename T> constexpr bool kCompactFilter = std::is_same<T, dfloat>::value;
 
 // Column passes keep the Boltzmann-factor tile of their output (N rows x 64
 // floats) in shared memory after the twiddle/gain tables.
@@ -165,9 +48,6 @@ template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_
   return ((fast_core_smem<T, N, XP>() + (size_t)N * 3 * sizeof(T) + 15) / 16) * 16;
 }
 
-__device__ __forceinline__ uint32_t smem_addr(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
 
 template <typename T, int N, int P, bool XP>
 __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps) {
