@@ -95,6 +95,13 @@ typedef struct scft_params {
 #define SCFT_FLAG_AUTOTUNE 32     /* time every legal schedule at creation and keep the fastest */
 #define SCFT_FLAG_NO_FUSED_STEPS 64 /* two-stream chains: two launches per contour step instead of
                                        one fused kernel per step pair (k_zz / k_xyxy) */
+#define SCFT_FLAG_PIN_TRANSLATION 256 /* Anderson mixing: remove from every field update its
+                                     component along the fields' rigid shifts (central-
+                                     difference gradients, least squares over both fields),
+                                     so the iteration cannot drift along the translational
+                                     zero mode and runs in different arithmetic from the
+                                     same start reach the same, unshifted structure (no
+                                     reference counterpart) */
 #define SCFT_FLAG_SIMPSON 128     /* phi contour sums with Simpson weights instead of the
                                      reference's trapezoid (w_to_phi_go, cuda_aid.cu:87-107):
                                      composite 1/3 rule, the 3/8 rule over the last three steps

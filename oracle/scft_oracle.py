@@ -635,10 +635,50 @@ def anderson_weights(G, c, hist, m1, err_max, start, lam, wopt):
     return a, lam
 
 
+def translation_generators(w):
+    """Rigid-shift directions of a field [b][Nz][Ny][Nx]: central differences
+    along x, y, z on the periodic grid, in grid units (None for a length-1
+    axis).  w(r - d) = w(r) - sum_a d_a t_a(r) + O(d^2)."""
+    out = []
+    for ax, n in ((3, w.shape[3]), (2, w.shape[2]), (1, w.shape[1])):
+        out.append(None if n == 1 else 0.5 * (np.roll(w, -1, axis=ax) - np.roll(w, 1, axis=ax)))
+    return out
+
+
+def remove_translation(wa0, wb0, wa1, wb1):
+    """The field update (wa0, wb0) -> (wa1, wb1) with its component along the
+    rigid shifts of (wa0, wb0) removed, per instance (least squares over both
+    fields: 3x3 normal equations of the generators).  Without it, an
+    iteration may drift along the translational zero mode (a converged
+    periodic structure is defined only up to a shift), and two runs of
+    different arithmetic drift differently."""
+    ta, tb = translation_generators(wa0), translation_generators(wb0)
+    axes = [k for k in range(3) if ta[k] is not None]
+    b = wa0.shape[0]
+    da, db = wa1 - wa0, wb1 - wb0
+    outa, outb = wa1.copy(), wb1.copy()
+    for bi in range(b):
+        n = len(axes)
+        G = np.empty((n, n))
+        c = np.empty(n)
+        for i, ai in enumerate(axes):
+            c[i] = (ta[ai][bi] * da[bi]).sum() + (tb[ai][bi] * db[bi]).sum()
+            for j, aj in enumerate(axes):
+                G[i, j] = (ta[ai][bi] * ta[aj][bi]).sum() + (tb[ai][bi] * tb[aj][bi]).sum()
+        G += np.eye(n) * (1e-14 * np.abs(np.diag(G)).max() + 1e-300)
+        alpha = np.linalg.solve(G, c)
+        for i, ai in enumerate(axes):
+            outa[bi] -= alpha[i] * ta[ai][bi]
+            outb[bi] -= alpha[i] * tb[ai][bi]
+    return outa, outb
+
+
 def converge_loop(wa, wb, p: Params, tol, max_it, mixing="anderson", m=20, lam=0.5,
-                  start=1e-2):
+                  start=1e-2, pin_translation=False):
     """Iterate Free's body (average_value x2, getConc, field update) until
-    max(err_max) < tol; returns (wa, wb, pha, phb, Q, iters, err_history)."""
+    max(err_max) < tol; returns (wa, wb, pha, phb, Q, iters, err_history).
+    pin_translation: each Anderson update without its rigid-shift component
+    (remove_translation), as the library's SCFT_FLAG_PIN_TRANSLATION."""
     kdz = kxyzdz_half(p)
     b = wa.shape[0]
     m1 = m + 1
@@ -677,8 +717,11 @@ def converge_loop(wa, wb, p: Params, tol, max_it, mixing="anderson", m=20, lam=0
                     if a[j] != 0.0:
                         new[bi] += a[j] * (hw[j][bi] + l * hd[j][bi])
             M = p.M
-            wa = new[:, :M].reshape(wa.shape)
-            wb = new[:, M:].reshape(wb.shape)
+            wa1 = new[:, :M].reshape(wa.shape)
+            wb1 = new[:, M:].reshape(wb.shape)
+            if pin_translation:
+                wa1, wb1 = remove_translation(wa, wb, wa1, wb1)
+            wa, wb = wa1, wb1
             count += 1
         if emax.max() < tol:
             break

@@ -48,7 +48,7 @@ EXPORTS = [
     "scft_shard_plan", "scft_free_shards",
 ]
 FLAG_NO_GRAPH, FLAG_PIPE, FLAG_TWO_STREAMS, FLAG_LOCKSTEP, FLAG_NO_XY = 1, 2, 4, 8, 16
-FLAG_AUTOTUNE, FLAG_NO_FUSED_STEPS, FLAG_SIMPSON = 32, 64, 128
+FLAG_AUTOTUNE, FLAG_NO_FUSED_STEPS, FLAG_SIMPSON, FLAG_PIN_TRANSLATION = 32, 64, 128, 256
 
 
 class ScftParams(C.Structure):

@@ -598,6 +598,14 @@ int mix(scft_ctx *ctx) {
   CKL(scft::launch_anderson_update(ctx->wa, ctx->wb, wj, dj, slots, hist + 1, ctx->and_a,
                                    ctx->and_lam, m1, M, B, ctx->st));
   ctx->launches += 4;   // residual: 4 kernels, Gram row: 2
+  if (ctx->p.flags & SCFT_FLAG_PIN_TRANSLATION) {
+    // the update without its rigid-shift component; ring slot c holds the
+    // pre-update fields
+    CKL(scft::launch_remove_translation(ctx->wa, ctx->wb, ctx->hist_w[c], ctx->p.nx, ctx->p.ny,
+                                        ctx->p.nz, B, ctx->rpartial, ctx->nblk, ctx->shift_alpha,
+                                        ctx->st));
+    ctx->launches += 2;
+  }
   ctx->and_count++;
   return SCFT_OK;
 }
@@ -662,6 +670,7 @@ void free_all(scft_ctx *ctx) {
   cudaFree(ctx->fe5); cudaFree(ctx->tables); cudaFree(ctx->dev_err);
   cudaFree(ctx->res); cudaFree(ctx->rpartial); cudaFree(ctx->gram); cudaFree(ctx->and_a);
   cudaFree(ctx->and_lam); cudaFree(ctx->target); cudaFree(ctx->dgain);
+  cudaFree(ctx->shift_alpha);
   scft_internal_adjoint_free(ctx);
   for (double *h : ctx->hist_w) cudaFree(h);
   for (double *h : ctx->hist_d) cudaFree(h);
@@ -844,7 +853,7 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     if (p.reserved[i]) return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "reserved fields must be 0");
   if (p.flags & ~(SCFT_FLAG_NO_GRAPH | SCFT_FLAG_PIPE | SCFT_FLAG_TWO_STREAMS |
                   SCFT_FLAG_LOCKSTEP | SCFT_FLAG_NO_XY | SCFT_FLAG_AUTOTUNE |
-                  SCFT_FLAG_NO_FUSED_STEPS | SCFT_FLAG_SIMPSON))
+                  SCFT_FLAG_NO_FUSED_STEPS | SCFT_FLAG_SIMPSON | SCFT_FLAG_PIN_TRANSLATION))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad flags");
   if (!(p.lx > 0 && p.ly > 0 && p.lz > 0 && p.ds0 > 0 && p.fA >= 0 && p.fA <= 1 && p.batch >= 1))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG, "bad box, ds0, fA or batch");
@@ -857,6 +866,9 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
       (p.anderson_history < 1 || p.anderson_history > 32 || !(p.anderson_lambda > 0)))
     return scft_fail(nullptr, SCFT_ERR_INVALID_ARG,
                      "Anderson history must be 1..32 and its step positive");
+  if ((p.flags & SCFT_FLAG_PIN_TRANSLATION) && p.mixing != SCFT_MIX_ANDERSON)
+    return scft_fail(nullptr, SCFT_ERR_INVALID_ARG,
+                     "SCFT_FLAG_PIN_TRANSLATION acts on Anderson updates: it needs SCFT_MIX_ANDERSON");
   if (!scft_grid_supported(p.nx, p.ny, p.nz))
     return scft_fail(nullptr, SCFT_ERR_UNSUPPORTED,
                      "grid unsupported: Nx must be even, Ny/Nz even or 1, each <= 4096 with "
@@ -934,6 +946,8 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
            alloc((void **)&ctx->hist_d[j], 8 * 2 * M * B);
     ok = ok && alloc((void **)&ctx->gram, 8 * B * ctx->m1 * ctx->m1) &&
          alloc((void **)&ctx->and_a, 8 * B * ctx->m1) && alloc((void **)&ctx->and_lam, 8 * B);
+    if (p.flags & SCFT_FLAG_PIN_TRANSLATION)
+      ok = ok && alloc((void **)&ctx->shift_alpha, 8 * 3 * B);
   }
   if (!ok) {
     cudaGetLastError();

@@ -54,6 +54,7 @@ struct scft_ctx {
   double *gram = nullptr;         // [batch][m1][m1]
   double *and_a = nullptr;        // [batch][m1] slot weights
   double *and_lam = nullptr;      // [batch] step
+  double *shift_alpha = nullptr;  // [batch][3] rigid-shift coefficients (SCFT_FLAG_PIN_TRANSLATION)
   long long and_count = 0;        // iterations stored in the ring
   double *target = nullptr;       // [batch][M] target phiA of the constrained updates
   // spectral tables (twiddles + gains of each pass), device

@@ -365,6 +365,122 @@ __global__ void k_anderson_update(double *__restrict__ wa, double *__restrict__ 
   }
 }
 
+// ---- the update without its rigid-shift component (SCFT_FLAG_PIN_TRANSLATION)
+// Rigid-shift generators of the pre-update fields w0 ([b][2][M], the Anderson
+// ring slot of this iteration): central differences along each axis longer
+// than one point, periodic, in grid units.
+struct Grid3 {
+  int nx, ny, nz;
+};
+__device__ __forceinline__ void shift_gen(const double *__restrict__ w0, long long i, Grid3 g,
+                                          double t[3]) {
+  const long long nxy = (long long)g.nx * g.ny;
+  const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / nxy);
+  const long long row = i - x, col = i - (long long)y * g.nx, pln = i - (long long)z * nxy;
+  t[0] = g.nx > 1 ? 0.5 * (w0[row + (x + 1) % g.nx] - w0[row + (x + g.nx - 1) % g.nx]) : 0.0;
+  t[1] = g.ny > 1 ? 0.5 * (w0[col + (long long)((y + 1) % g.ny) * g.nx] -
+                           w0[col + (long long)((y + g.ny - 1) % g.ny) * g.nx])
+                  : 0.0;
+  t[2] = g.nz > 1 ? 0.5 * (w0[pln + (long long)((z + 1) % g.nz) * nxy] -
+                           w0[pln + (long long)((z + g.nz - 1) % g.nz) * nxy])
+                  : 0.0;
+}
+
+// Per instance and block: the six Gram entries <t_a, t_b> and the three
+// projections <t_a, w1 - w0>, over both fields.
+// partial[(b*9 + k)*nblk + blk], k: G00 G01 G02 G11 G12 G22 c0 c1 c2
+__global__ void k_shift_dots(const double *__restrict__ wa1, const double *__restrict__ wb1,
+                             const double *__restrict__ w0, long long M, Grid3 g,
+                             double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const long long b = blockIdx.y;
+  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      const double *w0f = w0 + (2 * b + f) * M;
+      double t[3];
+      shift_gen(w0f, i, g, t);
+      const double d = (f ? wb1 : wa1)[b * M + i] - w0f[i];
+      acc[0] += t[0] * t[0];
+      acc[1] += t[0] * t[1];
+      acc[2] += t[0] * t[2];
+      acc[3] += t[1] * t[1];
+      acc[4] += t[1] * t[2];
+      acc[5] += t[2] * t[2];
+      acc[6] += t[0] * d;
+      acc[7] += t[1] * d;
+      acc[8] += t[2] * d;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const double r = blk_sum(acc[k], sh);
+    if (threadIdx.x == 0) partial[(b * 9 + k) * gridDim.x + blockIdx.x] = r;
+  }
+}
+
+// alpha[b*3 + a]: least-squares shift coefficients over the axes longer than
+// one point (the normal equations with a 1e-14 relative diagonal shift).
+__global__ void k_shift_solve(const double *__restrict__ partial, int nblk, Grid3 g,
+                              double *__restrict__ alpha) {
+  __shared__ double sh[32];
+  const int b = blockIdx.x;
+  double s[9];
+  for (int k = 0; k < 9; ++k) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < nblk; i += blockDim.x) v += partial[(b * 9 + k) * nblk + i];
+    s[k] = blk_sum(v, sh);
+  }
+  if (threadIdx.x != 0) return;
+  const double G[3][3] = {{s[0], s[1], s[2]}, {s[1], s[3], s[4]}, {s[2], s[4], s[5]}};
+  const int n3[3] = {g.nx, g.ny, g.nz};
+  int ax[3], n = 0;
+  for (int a = 0; a < 3; ++a)
+    if (n3[a] > 1) ax[n++] = a;
+  double A[3][4], dmax = 0.0;
+  for (int i = 0; i < n; ++i) dmax = fmax(dmax, fabs(G[ax[i]][ax[i]]));
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j < n; ++j) A[i][j] = G[ax[i]][ax[j]];
+    A[i][i] += 1e-14 * dmax + 1e-300;
+    A[i][3] = s[6 + ax[i]];
+  }
+  // Gaussian elimination (symmetric positive definite: no pivoting needed)
+  for (int k = 0; k < n; ++k)
+    for (int r = k + 1; r < n; ++r) {
+      const double f = A[r][k] / A[k][k];
+      for (int j = k; j < 4; ++j) A[r][j] -= f * A[k][j];
+    }
+  double x[3] = {0.0, 0.0, 0.0};
+  for (int i = n - 1; i >= 0; --i) {
+    double v = A[i][3];
+    for (int j = i + 1; j < n; ++j) v -= A[i][j] * x[j];
+    x[i] = v / A[i][i];
+  }
+  double out[3] = {0.0, 0.0, 0.0};
+  for (int i = 0; i < n; ++i) out[ax[i]] = x[i];
+  for (int a = 0; a < 3; ++a) alpha[b * 3 + a] = out[a];
+}
+
+// w1 -= sum_a alpha_a t_a(w0), both fields
+__global__ void k_shift_apply(double *__restrict__ wa1, double *__restrict__ wb1,
+                              const double *__restrict__ w0, long long M, Grid3 g,
+                              const double *__restrict__ alpha) {
+  const long long b = blockIdx.y;
+  const double a0 = alpha[b * 3], a1 = alpha[b * 3 + 1], a2 = alpha[b * 3 + 2];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M;
+       i += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      double t[3];
+      shift_gen(w0 + (2 * b + f) * M, i, g, t);
+      double *w1 = (f ? wb1 : wa1) + b * M;
+      w1[i] -= a0 * t[0] + a1 * t[1] + a2 * t[2];
+    }
+  }
+}
+
 inline int grid_for(long long n) {
   long long g = (n + kThreads - 1) / kThreads;
   if (g > 152 * 8) g = 152 * 8;
@@ -408,6 +524,17 @@ cudaError_t launch_anderson_solve(const double *G, const double *err, int c, int
                                   double start, double lambda, double wopt, int batch,
                                   double *a, double *lam, cudaStream_t st) {
   k_anderson_solve<<<batch, 32, 0, st>>>(G, err, c, hist, m1, start, lambda, wopt, a, lam);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_remove_translation(double *wa, double *wb, const double *w0, int nx, int ny,
+                                     int nz, int batch, double *partial, int nblk,
+                                     double *alpha, cudaStream_t st) {
+  const Grid3 g{nx, ny, nz};
+  const long long M = (long long)nx * ny * nz;
+  k_shift_dots<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, w0, M, g, partial);
+  k_shift_solve<<<batch, kThreads, 0, st>>>(partial, nblk, g, alpha);
+  k_shift_apply<<<dim3(grid_for(M), batch), kThreads, 0, st>>>(wa, wb, w0, M, g, alpha);
   return cudaGetLastError();
 }
 

@@ -104,6 +104,12 @@ cudaError_t launch_gram_row(const double *dc, const double *const *dj, const int
 cudaError_t launch_anderson_solve(const double *G, const double *err, int c, int hist, int m1,
                                   double start, double lambda, double wopt, int batch,
                                   double *a, double *lam, cudaStream_t st);
+// The update w0 -> (wa, wb) without its component along the rigid shifts of
+// w0 ([b][2][M], central differences, periodic): three kernels; partial holds
+// batch*9*nblk doubles, alpha batch*3.
+cudaError_t launch_remove_translation(double *wa, double *wb, const double *w0, int nx, int ny,
+                                     int nz, int batch, double *partial, int nblk,
+                                     double *alpha, cudaStream_t st);
 cudaError_t launch_anderson_update(double *wa, double *wb, const double *const *hw,
                                    const double *const *hd, const int *idx, int n,
                                    const double *a, const double *lam, int m1, long long M,

@@ -96,3 +96,57 @@ def test_bad_anderson_params(pkg):
     with pytest.raises(pkg.ScftError) as e:
         ctx_for(pkg, mixing=pkg.MIX_ANDERSON, anderson_history=40)
     assert e.value.status == pkg.ERR_INVALID_ARG
+
+
+def test_pinned_translation_trajectory_matches_oracle(pkg, orc):
+    """SCFT_FLAG_PIN_TRANSLATION: every Anderson update without its component
+    along the fields' rigid shifts, against the oracle's remove_translation
+    (the same least squares over both fields' central-difference gradients)."""
+    wa, wb = fields()
+    p = oparams(orc)
+    kw = dict(mixing=pkg.MIX_ANDERSON, anderson_history=10, anderson_lambda=0.5,
+              anderson_start=0.1, flags=pkg.FLAG_PIN_TRANSLATION)
+    with ctx_for(pkg, **kw) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.iterate(40)
+        ga, gb = ctx.wa, ctx.wb
+    ra, rb, *_ = orc.converge_loop(wa, wb, p, 1e-30, 40, mixing="anderson", m=10, lam=0.5,
+                                   start=0.1, pin_translation=True)
+    scale = np.abs(ra).max()
+    assert np.abs(ga - ra).max() / scale < 1e-7
+    assert np.abs(gb - rb).max() / scale < 1e-7
+    # the pinning changes the trajectory (else the test would not test it)
+    ua, *_ = orc.converge_loop(wa, wb, p, 1e-30, 40, mixing="anderson", m=10, lam=0.5,
+                               start=0.1)
+    assert np.abs(ua - ra).max() / scale > 1e-6
+
+
+def test_pinned_translation_fp32_df_polish_agrees_pointwise(pkg):
+    """With the rigid shifts pinned, FP32 propagation followed by the
+    double-float polish reaches the plain FP64 path's structure without any
+    alignment: phi pointwise within 1e-6 relative once both reach 1e-8."""
+    from scft_gb300 import fields as fl
+    g = dict(nx=64, ny=32, nz=32, lx=3.8, ly=3.8, lz=3.8, hAB=18.0, fA=0.36, ds0=0.01,
+             mixing=pkg.MIX_ANDERSON, anderson_history=20, anderson_start=1e9,
+             flags=pkg.FLAG_PIN_TRANSLATION)
+    wa, wb = fl.gyroid(64, 32, 32, 3.8, 3.8, 3.8, 18.0, seed=0)
+    with pkg.Context(precision=pkg.PREC_FP64, **g) as c64:
+        c64.set_w(wa, wb)
+        _, fe64 = c64.converge(1e-8, 2000)
+        pha64, phb64 = c64.pha, c64.phb
+    with pkg.Context(precision=pkg.PREC_FP32, **g) as c32, \
+            pkg.Context(precision=pkg.PREC_DF, **g) as cdf:
+        c32.set_w(wa, wb)
+        c32.converge(3e-5, 2000)
+        cdf.copy_fields_from(c32)
+        _, fedf = cdf.converge(1e-8, 2000)
+        phadf, phbdf = cdf.pha, cdf.phb
+    assert abs(fedf[0, 0] - fe64[0, 0]) < 1e-9
+    assert np.abs(phadf - pha64).max() / np.abs(pha64).max() < 1e-6
+    assert np.abs(phbdf - phb64).max() / np.abs(phb64).max() < 1e-6
+
+
+def test_pin_translation_needs_anderson(pkg):
+    with pytest.raises(pkg.ScftError) as e:
+        ctx_for(pkg, flags=pkg.FLAG_PIN_TRANSLATION)
+    assert e.value.status == pkg.ERR_INVALID_ARG

@@ -216,3 +216,25 @@ def test_contour_weights(orc):
     rng = np.random.default_rng(0)
     q, qc = rng.random((2, 2, 8, 3, 4))
     np.testing.assert_allclose(orc.contour_sum(q, qc), orc.trapezoid_sum(q, qc), rtol=1e-15)
+
+
+def test_remove_translation_removes_a_pure_shift():
+    """An update that is a small rigid shift of the fields (plus nothing else)
+    is removed to first order; an update orthogonal to the shifts is kept."""
+    from oracle import scft_oracle as orc
+    n = 16
+    x = np.arange(n) * 2 * np.pi / n
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    wa = (np.sin(X) * np.cos(Y) + np.sin(Y) * np.cos(Z) + np.sin(Z) * np.cos(X))[None]
+    wb = -wa
+    ta = orc.translation_generators(wa)
+    tb = orc.translation_generators(wb)
+    d = 1e-3
+    a1, b1 = orc.remove_translation(wa, wb, wa - d * (ta[0] + 2 * ta[1]),
+                                    wb - d * (tb[0] + 2 * tb[1]))
+    assert np.abs(a1 - wa).max() < 1e-14 and np.abs(b1 - wb).max() < 1e-14
+    # the uniform field is orthogonal to every central difference
+    a2, b2 = orc.remove_translation(wa, wb, wa + 0.5, wb - 0.25)
+    assert np.allclose(a2 - wa, 0.5, atol=1e-14) and np.allclose(b2 - wb, -0.25, atol=1e-14)
+    # a length-1 axis has no generator
+    assert orc.translation_generators(wa[:, :1])[2] is None
