@@ -26,15 +26,73 @@ __device__ __forceinline__ void group_sync(int bar_id, int nthreads) {
   else asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(nthreads) : "memory");
 }
 
+// The tables four_step reads, laid out so that every access is a constant
+// offset from one per-thread base (shared memory, 16-byte aligned):
+//   tw[p*R1 + k1]     = W_N^(p*k1)          stage-1 twiddles of warp p
+//   tw[N + k1*P + q]  = conj(W_N^(q*k1))    stage-2 inverse twiddles of column k1
+//   gain[k1*P + k2]   = g[k1 + R1*k2]       the filter gain at X[k1 + R1*k2]
+// built from the natural tables tw_n[m] = W_N^m, g_n[m] (global memory) by
+// load_filter_tables.  (four_step_compact keeps the natural layout.)
+template <int N, int P, typename C, typename T>
+__device__ __forceinline__ void load_filter_tables(C *tw, T *gain, const C *tw_n, const T *g_n,
+                                                   int tid, int nthreads) {
+  constexpr int R1 = N / P;
+  for (int i = tid; i < N; i += nthreads) {
+    const int p = i / R1, k1 = i % R1;
+    tw[i] = ldg(tw_n + (p * k1) % N);
+    const int c = i / P, q = i % P;
+    tw[N + i] = cconj(ldg(tw_n + (q * c) % N));
+    gain[i] = ldg(g_n + c + R1 * q);
+  }
+}
+// The natural tables (four_step_compact).
+template <int N, typename C, typename T>
+__device__ __forceinline__ void load_natural_tables(C *tw, T *gain, const C *tw_n, const T *g_n,
+                                                    int tid, int nthreads) {
+  for (int i = tid; i < N; i += nthreads) {
+    tw[i] = ldg(tw_n + i);
+    gain[i] = ldg(g_n + i);
+  }
+}
+// Shared-memory reals the tables of a length-N filter take (either layout).
+template <int N> constexpr int filter_table_reals() { return 5 * N; }
+
+// Two consecutive complex table entries (one 16-byte load for FP32), and four
+// consecutive gains (one 16-byte load for FP32).
+template <typename C> __device__ __forceinline__ void ld_c2(const C *a, C &x, C &y) {
+  if constexpr (sizeof(C) == 8) {
+    const float4 t = *reinterpret_cast<const float4 *>(a);
+    x.x = t.x; x.y = t.y; y.x = t.z; y.y = t.w;
+  } else {
+    x = a[0];
+    y = a[1];
+  }
+}
+template <typename T> __device__ __forceinline__ void ld_r4(const T *a, T (&r)[4]) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 t = *reinterpret_cast<const float4 *>(a);
+    r[0] = t.x; r[1] = t.y; r[2] = t.z; r[3] = t.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r[i] = a[i];
+  }
+}
+
 template <int N, int P, typename C, typename T, typename F>
 __device__ __forceinline__ void four_step(C (&v)[N / P], C *ex, const C *tw, const T *gain, int p,
                                           int lane, int bar_id, F &&after_first_sync) {
   constexpr int R1 = N / P;
+  static_assert(R1 % 2 == 0 && P % 4 == 0, "table vector loads");
   reg::dft<R1, false>(v);
-  reg::static_for<0, R1>([&](auto k_) {
-    constexpr int k1 = decltype(k_)::value;
-    if (k1 > 0) v[k1] = cmul(v[k1], tw[p * k1]);
+  const C *t1 = tw + p * R1;
+  reg::static_for<0, R1 / 2>([&](auto h_) {
+    constexpr int k1 = 2 * decltype(h_)::value;
+    C wa, wb;
+    ld_c2(t1 + k1, wa, wb);
+    if (k1 > 0) v[k1] = cmul(v[k1], wa);
+    v[k1 + 1] = cmul(v[k1 + 1], wb);
     ex[(k1 * P + p) * 32 + lane] = v[k1];
+    ex[((k1 + 1) * P + p) * 32 + lane] = v[k1 + 1];
   });
   group_sync(bar_id, P * 32);
   after_first_sync();
@@ -45,17 +103,27 @@ __device__ __forceinline__ void four_step(C (&v)[N / P], C *ex, const C *tw, con
       u[q] = ex[(k1 * P + q) * 32 + lane];
     });
     reg::dft<P, false>(u);
-    reg::static_for<0, P>([&](auto k2_) {
-      constexpr int k2 = decltype(k2_)::value;
-      const T g = gain[k1 + R1 * k2];
-      u[k2].x *= g;
-      u[k2].y *= g;
+    const T *gk = gain + k1 * P;
+    reg::static_for<0, P / 4>([&](auto h_) {
+      constexpr int k2 = 4 * decltype(h_)::value;
+      T g[4];
+      ld_r4(gk + k2, g);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        u[k2 + i].x *= g[i];
+        u[k2 + i].y *= g[i];
+      }
     });
     reg::dft<P, true>(u);
-    reg::static_for<0, P>([&](auto q_) {
-      constexpr int q = decltype(q_)::value;
-      if (q > 0) u[q] = cmul(u[q], cconj(tw[q * k1]));
+    const C *t2 = tw + N + k1 * P;
+    reg::static_for<0, P / 2>([&](auto h_) {
+      constexpr int q = 2 * decltype(h_)::value;
+      C wa, wb;
+      ld_c2(t2 + q, wa, wb);
+      if (q > 0) u[q] = cmul(u[q], wa);
+      u[q + 1] = cmul(u[q + 1], wb);
       ex[(k1 * P + q) * 32 + lane] = u[q];
+      ex[(k1 * P + q + 1) * 32 + lane] = u[q + 1];
     });
   }
   group_sync(bar_id, P * 32);

@@ -45,7 +45,8 @@ template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_
 // Column passes keep the Boltzmann-factor tile of their output (N rows x 64
 // floats) in shared memory after the twiddle/gain tables.
 template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_wtile_off() {
-  return ((fast_core_smem<T, N, XP>() + (size_t)N * 3 * sizeof(T) + 15) / 16) * 16;
+  return ((fast_core_smem<T, N, XP>() + (size_t)filter_table_reals<N>() * sizeof(T) + 15) / 16) *
+         16;
 }
 
 
@@ -72,11 +73,13 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
   // on the previous pass, so this overlaps its tail, and the FFT stages then
   // read them with shared-memory broadcasts instead of dependent global loads.
   C *s_tw = reinterpret_cast<C *>(smem_raw + fast_core_smem<T, N, XP>());
-  T *s_g = reinterpret_cast<T *>(s_tw + N);
-  for (int i = threadIdx.x; i < N; i += NT) {
-    s_tw[i] = ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
-    s_g[i] = ldg(reinterpret_cast<const T *>(ap.gain) + i);
-  }
+  T *s_g = reinterpret_cast<T *>(s_tw + (kCompactFilter<T> ? N : 2 * N));
+  if constexpr (kCompactFilter<T>)
+    load_natural_tables<N>(s_tw, s_g, reinterpret_cast<const C *>(ap.twiddle),
+                           reinterpret_cast<const T *>(ap.gain), threadIdx.x, NT);
+  else
+    load_filter_tables<N, P>(s_tw, s_g, reinterpret_cast<const C *>(ap.twiddle),
+                             reinterpret_cast<const T *>(ap.gain), threadIdx.x, NT);
   // Column passes with a post factor: the factor's tile does not depend on
   // the previous pass either, so its cp.async copies are issued here too and
   // land while the lines are loaded and filtered (the epilogue then reads
@@ -251,11 +254,13 @@ __global__ void __launch_bounds__(P * 32, N <= 128 ? 2 : 1)
                     reinterpret_cast<float *>(smem_raw) + N * 64};
   float2 *ex = reinterpret_cast<float2 *>(smem_raw + 2 * kTileBytes);
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + 3 * kTileBytes);
+  float2 *tw = reinterpret_cast<float2 *>(smem_raw + 3 * kTileBytes + 16);
+  float *gain = reinterpret_cast<float *>(tw + 2 * N);
   const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
   const int ntx = ap.n_real / 64;
   const long long T = (long long)ps.nset * ps.batch * ap.n_outer * ntx;
-  const float2 *__restrict__ tw = reinterpret_cast<const float2 *>(ap.twiddle);
-  const float *__restrict__ gain = reinterpret_cast<const float *>(ap.gain);
+  load_filter_tables<N, P>(tw, gain, reinterpret_cast<const float2 *>(ap.twiddle),
+                           reinterpret_cast<const float *>(ap.gain), threadIdx.x, P * 32);
 
   struct Tile {
     const float *in;
@@ -347,7 +352,9 @@ __global__ void __launch_bounds__(P * 32, N <= 128 ? 2 : 1)
   }
 }
 
-template <int N, int P> size_t pipe_smem() { return (size_t)3 * N * 64 * 4 + 16; }
+template <int N, int P> size_t pipe_smem() {
+  return (size_t)3 * N * 64 * 4 + 16 + (size_t)filter_table_reals<N>() * 4;
+}
 
 // ------------------------------------------------------------------------
 // Fused x+y pass: one CTA per z-plane.  The plane (NY rows, pitch NX+1) sits
@@ -364,7 +371,7 @@ template <int NX, int NY> constexpr size_t xy_plane_bytes() {
 // of independent work in flight per plane.
 template <int NX, int NY, int G> constexpr size_t xy_smem() {
   return xy_plane_bytes<NX, NY>() + (size_t)G * (NX > NY ? NX : NY) * 32 * 8 +
-         (size_t)(NX + NY) * 12;
+         (size_t)(filter_table_reals<NX>() + filter_table_reals<NY>()) * 4;
 }
 
 template <int NX, int NY, int G>
@@ -377,8 +384,8 @@ __global__ void __launch_bounds__(256 * G, G == 1 ? 2 : 1)
   float2 *ex0 = reinterpret_cast<float2 *>(smem_raw + xy_plane_bytes<NX, NY>());
   float2 *ex = ex0 + grp * (NX > NY ? NX : NY) * 32;
   float2 *twx = ex0 + G * (NX > NY ? NX : NY) * 32;
-  float2 *twy = twx + NX;
-  float *gx = reinterpret_cast<float *>(twy + NY);
+  float2 *twy = twx + 2 * NX;
+  float *gx = reinterpret_cast<float *>(twy + 2 * NY);
   float *gy = gx + NX;
   const int lane = threadIdx.x & 31, p = (threadIdx.x >> 5) & 7;
   const int bar_id = G == 1 ? 0 : 1 + grp;
@@ -391,14 +398,10 @@ __global__ void __launch_bounds__(256 * G, G == 1 ? 2 : 1)
   const float *post = set ? ps.post[1] : ps.post[0];
   if (pre) pre += b * ps.w_bs + base;
   if (post) post += b * ps.w_bs + base;
-  for (int i = threadIdx.x; i < NX; i += NT) {
-    twx[i] = __ldg(reinterpret_cast<const float2 *>(apx.twiddle) + i);
-    gx[i] = __ldg(reinterpret_cast<const float *>(apx.gain) + i);
-  }
-  for (int i = threadIdx.x; i < NY; i += NT) {
-    twy[i] = __ldg(reinterpret_cast<const float2 *>(apy.twiddle) + i);
-    gy[i] = __ldg(reinterpret_cast<const float *>(apy.gain) + i);
-  }
+  load_filter_tables<NX, P>(twx, gx, reinterpret_cast<const float2 *>(apx.twiddle),
+                            reinterpret_cast<const float *>(apx.gain), threadIdx.x, NT);
+  load_filter_tables<NY, P>(twy, gy, reinterpret_cast<const float2 *>(apy.twiddle),
+                            reinterpret_cast<const float *>(apy.gain), threadIdx.x, NT);
   // The Boltzmann factor does not depend on the previous pass: its loads are
   // issued before the dependency wait and overlap that pass's tail.  Then
   // every load of the plane is in flight at once (NX*NY/NT per thread):
@@ -483,11 +486,13 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<T> ps) {
   T *__restrict__ qo = ps.qout[set];
   const T *__restrict__ w = ps.post[set];
   C *s_tw = reinterpret_cast<C *>(smem_raw + fast_core_smem<T, N, false>());
-  T *s_g = reinterpret_cast<T *>(s_tw + N);
-  for (int i = threadIdx.x; i < N; i += NT) {
-    s_tw[i] = ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
-    s_g[i] = ldg(reinterpret_cast<const T *>(ap.gain) + i);
-  }
+  T *s_g = reinterpret_cast<T *>(s_tw + (kCompactFilter<T> ? N : 2 * N));
+  if constexpr (kCompactFilter<T>)
+    load_natural_tables<N>(s_tw, s_g, reinterpret_cast<const C *>(ap.twiddle),
+                           reinterpret_cast<const T *>(ap.gain), threadIdx.x, NT);
+  else
+    load_filter_tables<N, P>(s_tw, s_g, reinterpret_cast<const C *>(ap.twiddle),
+                             reinterpret_cast<const T *>(ap.gain), threadIdx.x, NT);
   T *s_wt = reinterpret_cast<T *>(smem_raw + fast_wtile_off<T, N, false>());
   const long long tile = (long long)blockIdx.y * ap.s_outer + (long long)blockIdx.x * 64;
   {
@@ -571,11 +576,13 @@ __global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<T> ps) {
   const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
   const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
   C *s_tw = reinterpret_cast<C *>(smem_raw + fast_core_smem<T, N, true>());
-  T *s_g = reinterpret_cast<T *>(s_tw + N);
-  for (int i = threadIdx.x; i < N; i += NT) {
-    s_tw[i] = ldg(reinterpret_cast<const C *>(ap.twiddle) + i);
-    s_g[i] = ldg(reinterpret_cast<const T *>(ap.gain) + i);
-  }
+  T *s_g = reinterpret_cast<T *>(s_tw + (kCompactFilter<T> ? N : 2 * N));
+  if constexpr (kCompactFilter<T>)
+    load_natural_tables<N>(s_tw, s_g, reinterpret_cast<const C *>(ap.twiddle),
+                           reinterpret_cast<const T *>(ap.gain), threadIdx.x, NT);
+  else
+    load_filter_tables<N, P>(s_tw, s_g, reinterpret_cast<const C *>(ap.twiddle),
+                             reinterpret_cast<const T *>(ap.gain), threadIdx.x, NT);
   const long long base = (long long)blockIdx.x * 64 * N;   // 64 consecutive rows
   T *s_wt = reinterpret_cast<T *>(smem_raw + xx_wtile_off<T, N>());
   {
@@ -657,7 +664,8 @@ template <int NX, int NY> constexpr size_t xyxy_wplane_off() {
 }
 template <int NX, int NY, int G> constexpr size_t xyxy_smem() {
   return xy_plane_bytes<NX, NY>() + (size_t)NX * NY * 4 +
-         (size_t)G * (NX > NY ? NX : NY) * 32 * 8 + (size_t)(NX + NY) * 12;
+         (size_t)G * (NX > NY ? NX : NY) * 32 * 8 +
+         (size_t)(filter_table_reals<NX>() + filter_table_reals<NY>()) * 4;
 }
 
 template <int NX, int NY, int G>
@@ -672,8 +680,8 @@ __global__ void __launch_bounds__(256 * G, 1)
                                            (size_t)NX * NY * 4);
   float2 *ex = ex0 + grp * (NX > NY ? NX : NY) * 32;
   float2 *twx = ex0 + G * (NX > NY ? NX : NY) * 32;
-  float2 *twy = twx + NX;
-  float *gx = reinterpret_cast<float *>(twy + NY);
+  float2 *twy = twx + 2 * NX;
+  float *gx = reinterpret_cast<float *>(twy + 2 * NY);
   float *gy = gx + NX;
   const int lane = threadIdx.x & 31, p = (threadIdx.x >> 5) & 7;
   const int bar_id = G == 1 ? 0 : 1 + grp;
@@ -684,14 +692,10 @@ __global__ void __launch_bounds__(256 * G, 1)
   float *out = ps.out[set] + b * ps.out_bs[set] + base;
   float *qo = ps.qout[set] + b * ps.qout_bs[set] + base;
   const float *w = ps.post[set] + b * ps.w_bs + base;
-  for (int i = threadIdx.x; i < NX; i += NT) {
-    twx[i] = __ldg(reinterpret_cast<const float2 *>(apx.twiddle) + i);
-    gx[i] = __ldg(reinterpret_cast<const float *>(apx.gain) + i);
-  }
-  for (int i = threadIdx.x; i < NY; i += NT) {
-    twy[i] = __ldg(reinterpret_cast<const float2 *>(apy.twiddle) + i);
-    gy[i] = __ldg(reinterpret_cast<const float *>(apy.gain) + i);
-  }
+  load_filter_tables<NX, P>(twx, gx, reinterpret_cast<const float2 *>(apx.twiddle),
+                            reinterpret_cast<const float *>(apx.gain), threadIdx.x, NT);
+  load_filter_tables<NY, P>(twy, gy, reinterpret_cast<const float2 *>(apy.twiddle),
+                            reinterpret_cast<const float *>(apy.gain), threadIdx.x, NT);
   for (int c = threadIdx.x; c < NX * NY / 4; c += NT)
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(wplane + 4 * c)),
                  "l"(w + 4 * c)
@@ -767,7 +771,7 @@ __global__ void __launch_bounds__(256 * G, 1)
 }
 
 template <typename T, int N, int P, bool XP> size_t fast_smem() {
-  return XP ? fast_core_smem<T, N, XP>() + (size_t)N * 3 * sizeof(T)
+  return XP ? fast_core_smem<T, N, XP>() + (size_t)filter_table_reals<N>() * sizeof(T)
             : fast_wtile_off<T, N, XP>() + (size_t)N * 64 * sizeof(T);
 }
 
