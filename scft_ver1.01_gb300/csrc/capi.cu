@@ -753,6 +753,69 @@ int autotune(scft_ctx *ctx) {
 
 // Hooks for the group graph (group.cu).
 int scft_internal_pre_mix(scft_ctx *ctx) { return pre_mix(ctx); }
+
+// Pieces of pre_mix for the group's batched march (group.cu): everything
+// before the march phase (average_value x3, the Boltzmann factors), the march
+// phase alone, and everything after it (Q, phi).
+int scft_internal_pre_march(scft_ctx *ctx) {
+  int rc;
+  if ((rc = average(ctx, ctx->wa))) return rc;   // cuda_scft.cu:170
+  if ((rc = average(ctx, ctx->wb))) return rc;   // :172
+  if ((rc = average(ctx, ctx->wa))) return rc;   // getConc, :71
+  if ((rc = boltzmann(ctx, SCFT_FIELD_WA, ctx->st))) return rc;
+  return boltzmann(ctx, SCFT_FIELD_WB, ctx->st);
+}
+int scft_internal_march(scft_ctx *ctx) { return march_phase_graph(ctx); }
+int scft_internal_post_march(scft_ctx *ctx) {
+  const int rc = with_real(ctx, [&](auto r) { return q_and_phi<decltype(r)>(ctx); });
+  ctx->have_conc = rc == SCFT_OK;
+  return rc;
+}
+
+namespace {
+// The two march chains of getConc as march_phase runs them.
+void chain_segs(const scft_ctx *ctx, int chain, Seg out[2]) {
+  if (chain == 0) {
+    out[0] = {SCFT_Q_A, SCFT_FIELD_WA, -1, 0, ctx->NsA, 1};
+    out[1] = {SCFT_Q_B, SCFT_FIELD_WB, SCFT_Q_A, ctx->NsA, ctx->dNsB, 1};
+  } else {
+    out[0] = {SCFT_Q_CB, SCFT_FIELD_WB, -1, 0, ctx->dNsB, -1};
+    out[1] = {SCFT_Q_CA, SCFT_FIELD_WA, SCFT_Q_CB, 0, ctx->NsA, -1};
+  }
+}
+}  // namespace
+
+// Contour step t (1-based) of march chain `chain` in lockstep order (the
+// run_chains schedule): whether the chain still marches at t, the slice it
+// reads and the slice it writes, the Boltzmann factor, and the segment whose
+// boundary slice must be set before the step (-1: none).  FP32 contexts.
+int scft_internal_chain_step(const scft_ctx *ctx, int chain, int t, int *active,
+                             const float **src, float **dst, const float **W, int *seg_start) {
+  Seg sg[2];
+  chain_segs(ctx, chain, sg);
+  *active = 0;
+  *seg_start = -1;
+  int k = 0, it = t;
+  if (t < 1 || t > sg[0].ns + sg[1].ns) return SCFT_OK;
+  while (it > sg[k].ns) it -= sg[k++].ns;
+  const Seg &s = sg[k];
+  const long long M = ctx->M;
+  float *q = static_cast<float *>(ctx->q[s.qi]);
+  const int d = s.sign > 0 ? it : s.ns - it;
+  *active = 1;
+  *dst = q + (long long)d * M;
+  *src = q + (long long)(s.sign > 0 ? d - 1 : d + 1) * M;
+  *W = static_cast<const float *>(ctx->W[s.wf]);
+  if (it == 1) *seg_start = k;
+  return SCFT_OK;
+}
+
+// initilize_q / qInt copy of segment `seg` of chain `chain` (seg_boundary).
+int scft_internal_seg_boundary(scft_ctx *ctx, int chain, int seg, cudaStream_t st) {
+  Seg sg[2];
+  chain_segs(ctx, chain, sg);
+  return seg_boundary<float>(ctx, sg[seg], st);
+}
 int scft_internal_mix(scft_ctx *ctx) { return mix(ctx); }
 int scft_internal_get_conc(scft_ctx *ctx) { return get_conc(ctx); }
 
@@ -989,10 +1052,32 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
     if (tl > n_pairs) tl = n_pairs;
     ap.tl = tl;
     ap.use_fast = scft::fast_line_supported(ap, rb) ? 1 : 0;
-    if (ctx->rkind == kRealDF && !ap.use_fast)
+    // Column passes (y, z) tile 64 columns of one row.  When Nx is not a
+    // multiple of 64 they run over flattened columns instead: z over the whole
+    // (x, y) plane (contiguous), y over (x, z) (row c / Nx, outer stride
+    // Nx*Ny).  That gives grids such as 32^3 and 48^3 register passes on every
+    // axis (and with them the fused step pairs).
+    if (a != 0 && !ap.use_fast && p.nx % 4 == 0) {
+      AxisPlan flat = ap;
+      flat.n_outer = 1;
+      if (a == 2) {
+        flat.n_real = p.nx * p.ny;
+        flat.s_outer = 0;
+      } else {
+        flat.n_real = p.nx * p.nz;
+        flat.s_outer = (long long)p.nx * p.ny;
+        flat.flat_nx = p.nx;
+      }
+      if (scft::fast_line_supported(flat, rb)) {
+        ap = flat;
+        ap.use_fast = 1;
+      }
+    }
+    if (ctx->rkind == kRealDF && (!ap.use_fast || (n != 32 && n != 64 && n != 128)))
       return fail(SCFT_ERR_UNSUPPORTED,
-                  "double-float propagation needs register-resident passes: Nx of 64 or "
-                  "128, Ny and Nz of 1, 32, 64 or 128, Ny*Nz a multiple of 64");
+                  "double-float propagation needs register-resident passes: Nx of 32, 64 "
+                  "or 128, Ny and Nz of 1, 32, 64 or 128, Ny*Nz a multiple of 64, "
+                  "Nx*Nz and Nx*Ny multiples of 64 when Nx is 32");
     if (scft::line_filter_smem_bytes(ap, rb) > (size_t)scft::kLineSmemMax)
       return fail(SCFT_ERR_UNSUPPORTED, "line too long for shared memory");
     // twiddles exp(-2 pi i m / n); the gains are filled by upload_gains

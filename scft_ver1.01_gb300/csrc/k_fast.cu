@@ -32,6 +32,15 @@ namespace {
 
 using namespace fcore;
 
+// Offset of column c (of a column pass's tile row) in one instance's grid:
+// the outer group blockIdx.y, or with flattened columns (ap.flat_nx) the row
+// c / flat_nx.  Two-real pairs and 16-byte copies never straddle rows
+// (flat_nx is a multiple of 4).
+__device__ __forceinline__ long long col_off(const AxisPlan &ap, long long c) {
+  if (ap.flat_nx) return (c / ap.flat_nx) * ap.s_outer + c % ap.flat_nx;
+  return (long long)blockIdx.y * ap.s_outer + c;
+}
+
 // Shared memory of k_fast_line before its tables: the exchange buffer
 // (N x 32 complex), or the 64-row staging tile (pitch N+1) of the x pass,
 // for real type T (float or double).
@@ -61,25 +70,37 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
   const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
   // blockIdx.z = set * batch + instance
   const int set = (int)blockIdx.z >= ps.batch ? 1 : 0;
-  const long long b = (long long)blockIdx.z - (long long)set * ps.batch;
-  const T *__restrict__ in = set ? ps.in[1] : ps.in[0];
-  T *__restrict__ out = set ? ps.out[1] : ps.out[0];
-  const T *__restrict__ pre = set ? ps.pre[1] : ps.pre[0];
-  const T *__restrict__ post = set ? ps.post[1] : ps.post[0];
+  long long b = (long long)blockIdx.z - (long long)set * ps.batch;
+  const T *in = set ? ps.in[1] : ps.in[0];
+  T *out = set ? ps.out[1] : ps.out[0];
+  const T *pre = set ? ps.pre[1] : ps.pre[0];
+  const T *post = set ? ps.post[1] : ps.post[0];
   const long long in_bs = set ? ps.in_bs[1] : ps.in_bs[0];
   const long long out_bs = set ? ps.out_bs[1] : ps.out_bs[0];
   const long long w_bs = ps.w_bs;
+  const T *gain_n = reinterpret_cast<const T *>(ap.gain);
+  if constexpr (std::is_same<T, float>::value) {
+    if (ps.desc) {   // a batched pass: this line set's own buffers and gains
+      const PassDesc d = ps.desc[blockIdx.z];
+      in = d.in;
+      out = d.out;
+      pre = d.pre;
+      post = d.post;
+      gain_n = d.gain;
+      b = 0;
+    }
+  }
   // The twiddle and gain tables go to shared memory first: they do not depend
   // on the previous pass, so this overlaps its tail, and the FFT stages then
   // read them with shared-memory broadcasts instead of dependent global loads.
   C *s_tw = reinterpret_cast<C *>(smem_raw + fast_core_smem<T, N, XP>());
   T *s_g = reinterpret_cast<T *>(s_tw + (kCompactFilter<T> ? N : 2 * N));
   if constexpr (kCompactFilter<T>)
-    load_natural_tables<N>(s_tw, s_g, reinterpret_cast<const C *>(ap.twiddle),
-                           reinterpret_cast<const T *>(ap.gain), threadIdx.x, NT);
+    load_natural_tables<N>(s_tw, s_g, reinterpret_cast<const C *>(ap.twiddle), gain_n,
+                           threadIdx.x, NT);
   else
-    load_filter_tables<N, P>(s_tw, s_g, reinterpret_cast<const C *>(ap.twiddle),
-                             reinterpret_cast<const T *>(ap.gain), threadIdx.x, NT);
+    load_filter_tables<N, P>(s_tw, s_g, reinterpret_cast<const C *>(ap.twiddle), gain_n,
+                             threadIdx.x, NT);
   // Column passes with a post factor: the factor's tile does not depend on
   // the previous pass either, so its cp.async copies are issued here too and
   // land while the lines are loaded and filtered (the epilogue then reads
@@ -88,13 +109,13 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
   if constexpr (!XP) {
     if (post) {
       constexpr int CPR = 64 / EPC;   // 16-byte copies per tile row of 64 reals
-      const T *wt = post + b * w_bs + (long long)blockIdx.y * ap.s_outer +
-                    (long long)blockIdx.x * 64;
+      const T *wt = post + b * w_bs;
       for (int c = threadIdx.x; c < N * CPR; c += NT) {
         const int row = c / CPR, part = c % CPR;
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
                          smem_addr(s_wt + row * 64 + part * EPC)),
-                     "l"(wt + (long long)row * ap.s_n + part * EPC)
+                     "l"(wt + col_off(ap, (long long)blockIdx.x * 64 + part * EPC) +
+                         (long long)row * ap.s_n)
                      : "memory");
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
@@ -127,7 +148,7 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
     });
     __syncthreads();
   } else {
-    base = (long long)blockIdx.y * ap.s_outer + (long long)blockIdx.x * 64 + 2 * lane;
+    base = col_off(ap, (long long)blockIdx.x * 64 + 2 * lane);
     const T *src = in + b * in_bs + base;
     reg::static_for<0, R1>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
@@ -398,10 +419,21 @@ __global__ void __launch_bounds__(256 * G, G == 1 ? 2 : 1)
   const float *post = set ? ps.post[1] : ps.post[0];
   if (pre) pre += b * ps.w_bs + base;
   if (post) post += b * ps.w_bs + base;
-  load_filter_tables<NX, P>(twx, gx, reinterpret_cast<const float2 *>(apx.twiddle),
-                            reinterpret_cast<const float *>(apx.gain), threadIdx.x, NT);
-  load_filter_tables<NY, P>(twy, gy, reinterpret_cast<const float2 *>(apy.twiddle),
-                            reinterpret_cast<const float *>(apy.gain), threadIdx.x, NT);
+  const float *gxn = reinterpret_cast<const float *>(apx.gain);
+  const float *gyn = reinterpret_cast<const float *>(apy.gain);
+  if (ps.desc) {   // a batched pass: this plane set's own buffers and gains
+    const PassDesc d = ps.desc[blockIdx.z];
+    in = d.in + base;
+    out = d.out + base;
+    pre = d.pre ? d.pre + base : nullptr;
+    post = d.post ? d.post + base : nullptr;
+    gxn = d.gain;
+    gyn = d.gain_y;
+  }
+  load_filter_tables<NX, P>(twx, gx, reinterpret_cast<const float2 *>(apx.twiddle), gxn,
+                            threadIdx.x, NT);
+  load_filter_tables<NY, P>(twy, gy, reinterpret_cast<const float2 *>(apy.twiddle), gyn,
+                            threadIdx.x, NT);
   // The Boltzmann factor does not depend on the previous pass: its loads are
   // issued before the dependency wait and overlap that pass's tail.  Then
   // every load of the plane is in flight at once (NX*NY/NT per thread):
@@ -810,7 +842,9 @@ template <typename T, int N, int P, bool XP> cudaError_t prep_one() {
 
 bool fast_line_supported(const AxisPlan &ap, size_t real_bytes) {
   // FP64 lines stop at 128 points (256 would not fit the registers)
-  if (ap.n != 32 && ap.n != 64 && ap.n != 128 && !(ap.n == 256 && real_bytes == 4)) return false;
+  if (ap.n != 32 && ap.n != 48 && ap.n != 64 && ap.n != 96 && ap.n != 128 &&
+      !(ap.n == 256 && real_bytes == 4))
+    return false;
   return ap.n_real % 64 == 0;
 }
 
@@ -913,7 +947,9 @@ cudaError_t launch_xx(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t
   if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
   switch (ap.n) {
     case 32: return launch_xx_t<float, 32, 4>(ap, ps, st);
+    case 48: return launch_xx_t<float, 48, 8>(ap, ps, st);
     case 64: return launch_xx_t<float, 64, 8>(ap, ps, st);
+    case 96: return launch_xx_t<float, 96, 8>(ap, ps, st);
     case 128: return launch_xx_t<float, 128, 8>(ap, ps, st);
     case 256: return launch_xx_t<float, 256, 16>(ap, ps, st);
     default: return cudaErrorInvalidValue;
@@ -929,8 +965,13 @@ cudaError_t launch_xx_wide(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_
     case 32: return launch_xx_t<T, 32, 4>(ap, ps, st);
     case 64: return launch_xx_t<T, 64, 8>(ap, ps, st);
     case 128: return launch_xx_t<T, 128, 8>(ap, ps, st);
-    default: return cudaErrorInvalidValue;
+    default: break;
   }
+  if constexpr (std::is_same<T, double>::value) {
+    if (ap.n == 48) return launch_xx_t<T, 48, 8>(ap, ps, st);
+    if (ap.n == 96) return launch_xx_t<T, 96, 8>(ap, ps, st);
+  }
+  return cudaErrorInvalidValue;
 }
 template <typename T>
 cudaError_t launch_zz_wide(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
@@ -940,8 +981,13 @@ cudaError_t launch_zz_wide(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_
     case 32: return launch_zz_t<T, 32, 4>(ap, ps, st);
     case 64: return launch_zz_t<T, 64, 8>(ap, ps, st);
     case 128: return launch_zz_t<T, 128, 8>(ap, ps, st);
-    default: return cudaErrorInvalidValue;
+    default: break;
   }
+  if constexpr (std::is_same<T, double>::value) {
+    if (ap.n == 48) return launch_zz_t<T, 48, 8>(ap, ps, st);
+    if (ap.n == 96) return launch_zz_t<T, 96, 8>(ap, ps, st);
+  }
+  return cudaErrorInvalidValue;
 }
 template <typename T>
 cudaError_t launch_fast_line_wide(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
@@ -959,8 +1005,15 @@ cudaError_t launch_fast_line_wide(const AxisPlan &ap, const PassSet<T> &ps, cuda
     case 128:
       return xp ? launch_one<T, 128, 8, true>(ap, ps, st)
                 : launch_one<T, 128, 8, false>(ap, ps, st);
-    default: return cudaErrorInvalidValue;
+    default: break;
   }
+  if constexpr (std::is_same<T, double>::value) {
+    if (ap.n == 48)
+      return xp ? launch_one<T, 48, 8, true>(ap, ps, st) : launch_one<T, 48, 8, false>(ap, ps, st);
+    if (ap.n == 96)
+      return xp ? launch_one<T, 96, 8, true>(ap, ps, st) : launch_one<T, 96, 8, false>(ap, ps, st);
+  }
+  return cudaErrorInvalidValue;
 }
 }  // namespace
 
@@ -981,7 +1034,9 @@ cudaError_t launch_zz(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t
   if (!fused_aligned(ps)) return cudaErrorMisalignedAddress;
   switch (ap.n) {
     case 32: return launch_zz_t<float, 32, 4>(ap, ps, st);
+    case 48: return launch_zz_t<float, 48, 8>(ap, ps, st);
     case 64: return launch_zz_t<float, 64, 8>(ap, ps, st);
+    case 96: return launch_zz_t<float, 96, 8>(ap, ps, st);
     case 128: return launch_zz_t<float, 128, 8>(ap, ps, st);
     case 256: return launch_zz_t<float, 256, 16>(ap, ps, st);
     default: return cudaErrorInvalidValue;
@@ -1029,6 +1084,10 @@ cudaError_t fast_line_prepare() {
   PREP(float, 64, 8)
   PREP(float, 128, 8)
   PREP(float, 256, 16)
+  PREP(float, 48, 8)
+  PREP(float, 96, 8)
+  PREP(double, 48, 8)
+  PREP(double, 96, 8)
   PREP(double, 32, 4)
   PREP(double, 64, 8)
   PREP(double, 128, 8)
@@ -1058,6 +1117,10 @@ cudaError_t fast_line_prepare() {
   PREP_FUSED(float, 64, 8)
   PREP_FUSED(float, 128, 8)
   PREP_FUSED(float, 256, 16)
+  PREP_FUSED(float, 48, 8)
+  PREP_FUSED(float, 96, 8)
+  PREP_FUSED(double, 48, 8)
+  PREP_FUSED(double, 96, 8)
   PREP_FUSED(double, 32, 4)
   PREP_FUSED(double, 64, 8)
   PREP_FUSED(double, 128, 8)
@@ -1079,7 +1142,7 @@ cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaS
   const bool xp = ap.n_fast != 0;
   // column passes: the persistent pipelined kernel when the caller supplied
   // an error word for its bounded waits
-  if (!xp && ps.err) {
+  if (!xp && ps.err && !ap.flat_nx) {
     switch (ap.n) {
       case 32: return launch_pipe<32, 4>(ap, ps, st, 0);
       case 64: return launch_pipe<64, 8>(ap, ps, st, 1);
@@ -1101,6 +1164,12 @@ cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaS
     case 256:
       return xp ? launch_one<float, 256, 16, true>(ap, ps, st)
                 : launch_one<float, 256, 16, false>(ap, ps, st);
+    case 48:
+      return xp ? launch_one<float, 48, 8, true>(ap, ps, st)
+                : launch_one<float, 48, 8, false>(ap, ps, st);
+    case 96:
+      return xp ? launch_one<float, 96, 8, true>(ap, ps, st)
+                : launch_one<float, 96, 8, false>(ap, ps, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -14,6 +14,8 @@
 // Tile: tl complex lines (2*tl real lines) of one outer group live in shared
 // memory as two ping-pong buffers; each Stockham stage of radix p reads one
 // buffer and writes the other (autosort, natural order in and out).
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -164,7 +166,8 @@ template <typename R>
 __global__ void __launch_bounds__(256) k_line_filter(AxisPlan ap, const R *__restrict__ in,
                                                      long long in_bs, R *__restrict__ out,
                                                      long long out_bs, const R *__restrict__ pre,
-                                                     const R *__restrict__ post, long long w_bs) {
+                                                     const R *__restrict__ post, long long w_bs,
+                                                     const PassDesc *desc) {
   typedef typename cplx<R>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = ap.n;
@@ -186,6 +189,16 @@ __global__ void __launch_bounds__(256) k_line_filter(AxisPlan ap, const R *__res
   R *outb = out + (long long)b * out_bs + base;
   const R *preb = pre ? pre + (long long)b * w_bs + base : nullptr;
   const R *postb = post ? post + (long long)b * w_bs + base : nullptr;
+  if constexpr (std::is_same<R, float>::value) {
+    if (desc) {   // a batched pass: this line set's own buffers and gains
+      const PassDesc d = desc[b];
+      inb = d.in + base;
+      outb = d.out + base;
+      preb = d.pre ? d.pre + base : nullptr;
+      postb = d.post ? d.post + base : nullptr;
+      gain = d.gain;
+    }
+  }
 
   // ---- load (two real lines -> one complex line)
   const int total = tl * 2 * n;
@@ -257,7 +270,19 @@ cudaError_t launch_line_filter(const AxisPlan &ap, const R *in, long long in_bst
   dim3 grid((n_pairs + ap.tl - 1) / ap.tl, ap.n_outer, batch);
   const size_t smem = line_filter_smem_bytes(ap, sizeof(R));
   return launch_pdl(k_line_filter<R>, grid, dim3(256), smem, st, ap, in, in_bstride, out,
-                    out_bstride, pre, post, w_bstride);
+                    out_bstride, pre, post, w_bstride, static_cast<const PassDesc *>(nullptr));
+}
+
+cudaError_t launch_line_filter_desc(const AxisPlan &ap, const PassDesc *desc, int n,
+                                    cudaStream_t st) {
+  if (!desc || n < 1 || n > 65535 || ap.n_outer > 65535) return cudaErrorInvalidValue;
+  const int n_pairs = (ap.n_real + 1) >> 1;
+  dim3 grid((n_pairs + ap.tl - 1) / ap.tl, ap.n_outer, n);
+  const size_t smem = line_filter_smem_bytes(ap, sizeof(float));
+  return launch_pdl(k_line_filter<float>, grid, dim3(256), smem, st, ap,
+                    static_cast<const float *>(nullptr), 0LL, static_cast<float *>(nullptr), 0LL,
+                    static_cast<const float *>(nullptr), static_cast<const float *>(nullptr), 0LL,
+                    desc);
 }
 
 template cudaError_t launch_line_filter<float>(const AxisPlan &, const float *, long long, float *,

@@ -23,6 +23,9 @@ struct AxisPlan {
   int n_real;            // real lines per outer group (paired 2 by 2)
   int n_outer;           // outer groups per instance
   int n_fast;            // 1: consecutive threads walk n (contiguous lines)
+  int flat_nx;           // column passes: 0, or the row length when the columns run over a
+                         // flattened (row, outer) index: column c sits at
+                         // (c / flat_nx) * s_outer + c % flat_nx (n_outer 1)
   int tl;                // complex lines per CTA tile
   int use_fast;          // FP32 register-resident kernel (k_fast.cu) handles this pass
   const void *twiddle;   // device: n complex, exp(-2*pi*i*m/n), working precision
@@ -33,6 +36,15 @@ struct AxisPlan {
 // march chains): set k reads in[k] (+ b*in_bs), multiplies by pre[k], filters,
 // multiplies by post[k] and writes out[k] (+ b*out_bs), for every instance b.
 constexpr int kMaxSet = 2;
+// One line set of a batched pass over several contexts (a group's lockstep
+// march, FP32): the set's buffers (one instance each) and gain tables.
+struct PassDesc {
+  const float *in;
+  float *out;
+  const float *pre, *post;   // Boltzmann factor on load / on store, or null
+  const float *gain;         // the set's gain table of this pass's axis (x for a plane pass)
+  const float *gain_y;       // x+y plane passes: the y axis's gain table
+};
 template <typename R> struct PassSet {
   const R *in[kMaxSet];
   R *out[kMaxSet];
@@ -47,6 +59,9 @@ template <typename R> struct PassSet {
   // propagator slice goes; `out` then receives the next step's intermediate
   R *qout[kMaxSet];
   long long qout_bs[kMaxSet];
+  // FP32 per-axis and x+y plane passes: when set, line set blockIdx.z takes
+  // its buffers and gains from desc[blockIdx.z] (nset 1, batch = sets)
+  const PassDesc *desc;
 };
 
 // Register-resident pass (k_fast.cu): n in {32, 64, 128, 256} (FP32) or
@@ -84,6 +99,9 @@ template <typename R>
 cudaError_t launch_line_filter(const AxisPlan &ap, const R *in, long long in_bstride, R *out,
                                long long out_bstride, const R *pre, const R *post,
                                long long w_bstride, int batch, cudaStream_t st);
+// The same over n line sets described by desc[0..n) (FP32, device memory).
+cudaError_t launch_line_filter_desc(const AxisPlan &ap, const PassDesc *desc, int n,
+                                    cudaStream_t st);
 
 size_t line_filter_smem_bytes(const AxisPlan &ap, size_t real_bytes);
 constexpr int kLineSmemMax = 200 * 1024;

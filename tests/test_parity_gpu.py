@@ -25,6 +25,7 @@ GRIDS = [
     (64, 64, 1, 4.0, 4.0, 2.0),
     (256, 64, 8, 8.0, 3.0, 2.0),      # x, y fast; z (N=8) generic
     (106, 106, 1, 21.2, 21.2, 2.0),   # the reference's out.vtk grid: radix 53, spacing 0.2
+    (96, 48, 32, 4.0, 3.0, 2.5),      # 96- and 48-point register lines, flattened y/z columns
 ]
 
 
@@ -155,7 +156,8 @@ def test_simpson_uniform_field_gives_the_block_fractions(pkg):
 
 # register-resident passes on every axis: Nx in {64, 128}, Ny and Nz in
 # {1, 32, 64, 128}, Ny*Nz a multiple of 64
-DF_GRIDS = [GRIDS[7], GRIDS[8], GRIDS[9], (64, 64, 64, 3.8, 3.8, 3.8), (128, 32, 64, 5.0, 3.0, 4.0)]
+DF_GRIDS = [GRIDS[7], GRIDS[8], GRIDS[9], (64, 64, 64, 3.8, 3.8, 3.8), (128, 32, 64, 5.0, 3.0, 4.0),
+            (32, 32, 32, 4.0, 4.0, 4.0)]   # flattened y and z columns (Nx = 32)
 
 
 @pytest.mark.parametrize("g", DF_GRIDS)
@@ -196,7 +198,7 @@ def test_double_float_simpson_parity(pkg, orc, g, fA, ds0):
 def test_double_float_limits(pkg):
     """Grids without register-resident passes on every axis are refused
     (status, no fallback)."""
-    for n in ((48, 48, 48), (32, 32, 32), (256, 64, 64)):
+    for n in ((48, 48, 48), (96, 32, 32), (256, 64, 64)):
         with pytest.raises(pkg.ScftError) as e:
             pkg.Context(nx=n[0], ny=n[1], nz=n[2], precision=pkg.PREC_DF)
         assert e.value.status == pkg.ERR_UNSUPPORTED
