@@ -23,7 +23,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 
 SOURCES = ["capi.cu", "io.cpp", "compat.cpp", "k_line.cu", "k_fields.cu", "k_fast.cu",
-           "k_anderson.cu", "group.cu", "noalloc.cu", "adjoint.cu", "spline.cu"]
+           "k_anderson.cu", "group.cu", "noalloc.cu", "adjoint.cu", "spline.cu",
+           "k_plane256.cu"]
 # Per-file extra flags: the spline's host arithmetic keeps the reference's
 # rounding (no FMA contraction by the host compiler, which aarch64 gcc does by
 # default).

@@ -1057,12 +1057,14 @@ cudaError_t launch_xyxy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<
   if (apx.n == 64 && apy.n == 64) return launch_xyxy_t<64, 64>(apx, apy, ps, st);
   if (apx.n == 128 && apy.n == 64) return launch_xyxy_t<128, 64>(apx, apy, ps, st);
   if (apx.n == 64 && apy.n == 128) return launch_xyxy_t<64, 128>(apx, apy, ps, st);
+  if (plane256_fusable(apx, apy)) return launch_xyxy256(apx, apy, ps, st);
   return cudaErrorInvalidValue;
 }
 
 bool xy_fusable(const AxisPlan &apx, const AxisPlan &apy) {
+  if (plane256_fusable(apx, apy)) return true;
   return apx.n_fast && !apy.n_fast && (apx.n == 64 || apx.n == 128) &&
-         (apy.n == 64 || apy.n == 128) && apy.s_n == apx.n;
+         (apy.n == 64 || apy.n == 128) && apy.s_n == apx.n && !apy.flat_nx;
 }
 
 cudaError_t launch_xy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
@@ -1072,6 +1074,7 @@ cudaError_t launch_xy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<fl
   if (apx.n == 64 && apy.n == 64) return launch_xy_t<64, 64>(apx, apy, ps, st);
   if (apx.n == 128 && apy.n == 64) return launch_xy_t<128, 64>(apx, apy, ps, st);
   if (apx.n == 64 && apy.n == 128) return launch_xy_t<64, 128>(apx, apy, ps, st);
+  if (plane256_fusable(apx, apy)) return launch_xy256(apx, apy, ps, st);
   return cudaErrorInvalidValue;
 }
 
@@ -1110,6 +1113,7 @@ cudaError_t fast_line_prepare() {
   if ((e = prep_xyxy<64, 64>()) != cudaSuccess) return e;
   if ((e = prep_xyxy<128, 64>()) != cudaSuccess) return e;
   if ((e = prep_xyxy<64, 128>()) != cudaSuccess) return e;
+  if ((e = plane256_prepare()) != cudaSuccess) return e;
 #define PREP_FUSED(T, N, P)                                          \
   if ((e = prep_xx<T, N, P>()) != cudaSuccess) return e;            \
   if ((e = prep_zz<T, N, P>()) != cudaSuccess) return e;

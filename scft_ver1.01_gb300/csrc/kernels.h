@@ -72,6 +72,15 @@ bool xy_fusable(const AxisPlan &apx, const AxisPlan &apy);
 cudaError_t launch_xy(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
                       cudaStream_t st);
 cudaError_t fast_line_prepare();
+// x+y passes of 256 x 256 planes (k_plane256.cu): a cluster of two CTAs per
+// plane, the y lines read across the pair through distributed shared memory;
+// launch_xy / launch_xyxy dispatch here for such planes.
+bool plane256_fusable(const AxisPlan &apx, const AxisPlan &apy);
+cudaError_t plane256_prepare();
+cudaError_t launch_xy256(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
+                         cudaStream_t st);
+cudaError_t launch_xyxy256(const AxisPlan &apx, const AxisPlan &apy, const PassSet<float> &ps,
+                           cudaStream_t st);
 // bounded-wait self-test: sets bit 4 of *err after `limit` clocks
 cudaError_t launch_wait_selftest(unsigned *err, long long limit, cudaStream_t st);
 cudaError_t launch_fast_line(const AxisPlan &ap, const PassSet<float> &ps, cudaStream_t st);

@@ -70,6 +70,9 @@ LONG_Z = [
     ((64, 64, 128, 3.8, 3.8, 3.8), (0, 1, 2)),
     ((128, 128, 128, 3.8, 3.8, 3.8), (0, 1, 2)),
     ((64, 32, 256, 3.0, 2.0, 8.0), (1,)),
+    # 256 x 256 planes: the two-CTA cluster plane kernels (segment start and
+    # end planes, fused plane pairs) around k_zz<float, 32, 4>
+    ((256, 256, 32, 8.0, 8.0, 2.0), (1,)),
 ]
 
 
