@@ -2,8 +2,9 @@
  * scft_capi.h -- C ABI of the GB300-native diblock-copolymer SCFT hot path.
  *
  * One opaque context = one GPU, `batch` independent SCFT instances of one
- * grid/parameter set (the reference's CUFFT_INFO + GPU_INFO, struct.h:19-125,
- * with its GPU_N split collapsed to one device).  All entry points return an
+ * grid/parameter set (the reference's CUFFT_INFO + GPU_INFO, struct.h:19-125).
+ * The reference's GPU_N split of the instances over devices is one context per
+ * device (scft_shard_plan, scft_free_shards).  All entry points return an
  * SCFT_* status code and never exit the process; scft_last_error() gives the
  * message of the last failure on a context.
  *
