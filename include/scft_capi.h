@@ -333,8 +333,8 @@ int scft_read_ab_txt(const char *path, scft_params *p, int *intag);
 int scft_save_checkpoint(scft_ctx *ctx, const char *path, int with_history);
 /* Restore a checkpoint into a context of the same grid and batch
  * (SCFT_ERR_INVALID_ARG otherwise).  The history is restored only when the
- * precision, mixing, history length, box, xN, fA and ds0 also match;
- * otherwise it restarts. */
+ * precision, mixing, history length, Anderson lambda, box, xN, fA and ds0
+ * also match; otherwise it restarts. */
 int scft_load_checkpoint(scft_ctx *ctx, const char *path);
 
 /* JSON-lines metrics: with a path set, every progress report of scft_free

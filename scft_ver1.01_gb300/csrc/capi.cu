@@ -548,9 +548,10 @@ int get_conc(scft_ctx *ctx) {
 }
 
 // The field update.  Simple mixing is phi_w (cuda_aid.cu:382-416) with its
-// residual reduced on the way; Anderson mixing stores (w, d) in the ring,
-// extends the FP64 Gram matrix by one row, solves the small least-squares
-// problem on the device and applies the mixed step.  No host round trip.
+// residual reduced on the way; Anderson mixing stores (w + lambda d, d) in the
+// ring, extends the FP64 Gram matrix by one row, solves the small
+// least-squares problem on the device and applies the mixed step.  No host
+// round trip.
 int mix(scft_ctx *ctx) {
   NvtxRange range("scft field update");
   const long long M = ctx->M;
@@ -561,8 +562,8 @@ int mix(scft_ctx *ctx) {
     if (!ctx->target)
       return scft_fail(ctx, SCFT_ERR_INVALID_ARG, "constrained mixing needs a target field");
     CKL(scft::launch_residual(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->p.wcmp, 0.0,
-                              M, B, nullptr, nullptr, ctx->rpartial, ctx->nblk, ctx->res,
-                              ctx->st));
+                              M, B, nullptr, nullptr, 0.0, nullptr, ctx->rpartial, ctx->nblk,
+                              ctx->res, ctx->st));
     CKL(scft::launch_phi_w_constrained(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->target,
                                        ctx->p.hAB, ctx->p.constraint_lambda,
                                        ctx->p.mixing == SCFT_MIX_CONSTRAINED_EX, M, B, ctx->st));
@@ -571,8 +572,8 @@ int mix(scft_ctx *ctx) {
   }
   if (ctx->p.mixing == SCFT_MIX_SIMPLE) {
     CKL(scft::launch_residual(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->p.wcmp,
-                              ctx->p.wopt, M, B, nullptr, nullptr, ctx->rpartial, ctx->nblk,
-                              ctx->res, ctx->st));
+                              ctx->p.wopt, M, B, nullptr, nullptr, 0.0, nullptr, ctx->rpartial,
+                              ctx->nblk, ctx->res, ctx->st));
     ctx->launches += 3;   // launch_residual issues four kernels
     return SCFT_OK;
   }
@@ -580,28 +581,28 @@ int mix(scft_ctx *ctx) {
   const int c = (int)(ctx->and_count % m1);
   const int hist = (int)(ctx->and_count < m ? ctx->and_count : m);
   CKL(scft::launch_residual(ctx->wa, ctx->wb, ctx->pha, ctx->phb, ctx->p.hAB, ctx->p.wcmp, 0.0,
-                            M, B, ctx->hist_w[c], ctx->hist_d[c], ctx->rpartial, ctx->nblk,
-                            ctx->res, ctx->st));
-  const double *dj[33], *wj[33];
+                            M, B, ctx->hist_u[c], ctx->hist_d[c], ctx->p.anderson_lambda,
+                            ctx->wprev, ctx->rpartial, ctx->nblk, ctx->res, ctx->st));
+  const void *dj[33], *uj[33];
   int slots[33];
   for (int k = 0; k <= hist; ++k) {
     const int j = ((c - k) % m1 + m1) % m1;
     slots[k] = j;
     dj[k] = ctx->hist_d[j];
-    wj[k] = ctx->hist_w[j];
+    uj[k] = ctx->hist_u[j];
   }
   CKL(scft::launch_gram_row(ctx->hist_d[c], dj, slots, hist + 1, c, m1, M, B, ctx->rpartial,
                             ctx->nblk, ctx->gram, ctx->st));
   CKL(scft::launch_anderson_solve(ctx->gram, ctx->res, c, hist, m1, ctx->p.anderson_start,
                                   ctx->p.anderson_lambda, ctx->p.wopt, B, ctx->and_a,
                                   ctx->and_lam, ctx->st));
-  CKL(scft::launch_anderson_update(ctx->wa, ctx->wb, wj, dj, slots, hist + 1, ctx->and_a,
-                                   ctx->and_lam, m1, M, B, ctx->st));
+  CKL(scft::launch_anderson_update(ctx->wa, ctx->wb, uj, ctx->hist_d[c], slots, hist + 1,
+                                   ctx->and_a, ctx->and_lam, m1, M, B, ctx->st));
   ctx->launches += 4;   // residual: 4 kernels, Gram row: 2
   if (ctx->p.flags & SCFT_FLAG_PIN_TRANSLATION) {
-    // the update without its rigid-shift component; ring slot c holds the
+    // the update without its rigid-shift component; wprev holds the
     // pre-update fields
-    CKL(scft::launch_remove_translation(ctx->wa, ctx->wb, ctx->hist_w[c], ctx->p.nx, ctx->p.ny,
+    CKL(scft::launch_remove_translation(ctx->wa, ctx->wb, ctx->wprev, ctx->p.nx, ctx->p.ny,
                                         ctx->p.nz, B, ctx->rpartial, ctx->nblk, ctx->shift_alpha,
                                         ctx->st));
     ctx->launches += 2;
@@ -672,10 +673,11 @@ void free_all(scft_ctx *ctx) {
   cudaFree(ctx->and_lam); cudaFree(ctx->target); cudaFree(ctx->dgain);
   cudaFree(ctx->shift_alpha);
   scft_internal_adjoint_free(ctx);
-  for (double *h : ctx->hist_w) cudaFree(h);
-  for (double *h : ctx->hist_d) cudaFree(h);
-  ctx->hist_w.clear();
+  for (float *h : ctx->hist_u) cudaFree(h);
+  for (float *h : ctx->hist_d) cudaFree(h);
+  ctx->hist_u.clear();
   ctx->hist_d.clear();
+  cudaFree(ctx->wprev);
   for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
   ctx->prof_events.clear();
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -1002,15 +1004,16 @@ int scft_create(const scft_params *pin, scft_ctx **out) {
        alloc((void **)&ctx->rpartial, 8 * B * scft::anderson_max_slots() * ctx->nblk);
   if (ok && p.mixing == SCFT_MIX_ANDERSON) {
     ctx->m1 = p.anderson_history + 1;
-    ctx->hist_w.assign(ctx->m1, nullptr);
+    ctx->hist_u.assign(ctx->m1, nullptr);
     ctx->hist_d.assign(ctx->m1, nullptr);
     for (int j = 0; ok && j < ctx->m1; ++j)
-      ok = alloc((void **)&ctx->hist_w[j], 8 * 2 * M * B) &&
+      ok = alloc((void **)&ctx->hist_u[j], 8 * 2 * M * B) &&
            alloc((void **)&ctx->hist_d[j], 8 * 2 * M * B);
     ok = ok && alloc((void **)&ctx->gram, 8 * B * ctx->m1 * ctx->m1) &&
-         alloc((void **)&ctx->and_a, 8 * B * ctx->m1) && alloc((void **)&ctx->and_lam, 8 * B);
+         alloc((void **)&ctx->and_a, 8 * B * ctx->m1) && alloc((void **)&ctx->and_lam, 8 * 2 * B);
     if (p.flags & SCFT_FLAG_PIN_TRANSLATION)
-      ok = ok && alloc((void **)&ctx->shift_alpha, 8 * 3 * B);
+      ok = ok && alloc((void **)&ctx->shift_alpha, 8 * 3 * B) &&
+           alloc((void **)&ctx->wprev, 8 * 2 * M * B);
   }
   if (!ok) {
     cudaGetLastError();

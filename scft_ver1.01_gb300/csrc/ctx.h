@@ -50,10 +50,13 @@ struct scft_ctx {
   double *res = nullptr;          // [batch][2]: residual max|d|, rms(d)
   double *rpartial = nullptr;     // [batch][33][nblk] reduction partials
   int m1 = 0;                     // Anderson ring slots (history + 1)
-  std::vector<double *> hist_w, hist_d;   // ring of [batch][2][M]
+  // ring of [batch][2][M] double-float pairs (hi, lo floats, 8 bytes a
+  // value): u = w + anderson_lambda d and the mean-free residual d
+  std::vector<float *> hist_u, hist_d;
+  double *wprev = nullptr;        // [batch][2][M] pre-update fields (SCFT_FLAG_PIN_TRANSLATION)
   double *gram = nullptr;         // [batch][m1][m1]
   double *and_a = nullptr;        // [batch][m1] slot weights
-  double *and_lam = nullptr;      // [batch] step
+  double *and_lam = nullptr;      // [2][batch]: step, mode (1 Anderson, 0 simple)
   double *shift_alpha = nullptr;  // [batch][3] rigid-shift coefficients (SCFT_FLAG_PIN_TRANSLATION)
   long long and_count = 0;        // iterations stored in the ring
   double *target = nullptr;       // [batch][M] target phiA of the constrained updates

@@ -249,13 +249,14 @@ int scft_write_vtk(scft_ctx *ctx, const char *path, int inst, const char *source
 // ---- binary FP64 checkpoint (no reference counterpart) -------------------
 //
 // Layout (native byte order; both machines this builds for are little-endian):
-//   char[8] "SCFTCKP1", int32 version (1),
+//   char[8] "SCFTCKP2", int32 version (2),
 //   int32 nx, ny, nz, batch, precision, mixing, anderson_history, has_history,
-//   double lx, ly, lz, hAB, fA, ds0, int64 and_count,
+//   double lx, ly, lz, hAB, fA, ds0, int64 and_count, double anderson_lambda,
 //   double wa, wb, phiA, phiB   [batch][M] each,
 //   double residual             [batch][4]   (norms and means of the last update)
-//   with has_history: int32 m1, then m1 rings of w and m1 rings of d
-//   ([batch][2][M] each) and the Gram matrix [batch][m1][m1].
+//   with has_history: int32 m1, then m1 rings of u = w + anderson_lambda d and
+//   m1 rings of d ([batch][2][M] double-float pairs each: float hi, float lo,
+//   the device ring's bytes) and the Gram matrix [batch][m1][m1] (double).
 namespace {
 
 struct CkptHeader {
@@ -263,29 +264,33 @@ struct CkptHeader {
   int32_t version, nx, ny, nz, batch, precision, mixing, history, has_history;
   double lx, ly, lz, hAB, fA, ds0;
   int64_t and_count;
+  double anderson_lambda;
 };
 
-// device <-> file through a bounded host buffer
-int dev_to_file(scft_ctx *ctx, FILE *fp, const double *dev, long long n) {
-  const long long chunk = 1LL << 23;   // 64 MB of doubles
-  std::vector<double> buf((size_t)(n < chunk ? n : chunk));
+// device <-> file through a bounded host buffer, n 8-byte words copied as
+// bytes (doubles, or double-float pairs)
+int dev_to_file(scft_ctx *ctx, FILE *fp, const void *dev, long long n) {
+  const long long chunk = 1LL << 23;   // 64 MB
+  std::vector<uint64_t> buf((size_t)(n < chunk ? n : chunk));
+  const uint64_t *src = static_cast<const uint64_t *>(dev);
   for (long long o = 0; o < n; o += chunk) {
     const long long k = n - o < chunk ? n - o : chunk;
-    cudaError_t e = cudaMemcpy(buf.data(), dev + o, sizeof(double) * k, cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpy(buf.data(), src + o, 8 * k, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return scft_fail(ctx, SCFT_ERR_CUDA, cudaGetErrorString(e));
-    if (fwrite(buf.data(), sizeof(double), (size_t)k, fp) != (size_t)k)
+    if (fwrite(buf.data(), 8, (size_t)k, fp) != (size_t)k)
       return scft_fail(ctx, SCFT_ERR_IO, "checkpoint write failed");
   }
   return SCFT_OK;
 }
-int file_to_dev(scft_ctx *ctx, FILE *fp, double *dev, long long n) {
+int file_to_dev(scft_ctx *ctx, FILE *fp, void *dev, long long n) {
   const long long chunk = 1LL << 23;
-  std::vector<double> buf((size_t)(n < chunk ? n : chunk));
+  std::vector<uint64_t> buf((size_t)(n < chunk ? n : chunk));
+  uint64_t *dst = static_cast<uint64_t *>(dev);
   for (long long o = 0; o < n; o += chunk) {
     const long long k = n - o < chunk ? n - o : chunk;
-    if (fread(buf.data(), sizeof(double), (size_t)k, fp) != (size_t)k)
+    if (fread(buf.data(), 8, (size_t)k, fp) != (size_t)k)
       return scft_fail(ctx, SCFT_ERR_IO, "checkpoint file is short");
-    cudaError_t e = cudaMemcpy(dev + o, buf.data(), sizeof(double) * k, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpy(dst + o, buf.data(), 8 * k, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return scft_fail(ctx, SCFT_ERR_CUDA, cudaGetErrorString(e));
   }
   return SCFT_OK;
@@ -293,7 +298,7 @@ int file_to_dev(scft_ctx *ctx, FILE *fp, double *dev, long long n) {
 
 bool history_kept(const scft_ctx *ctx) {
   return ctx->p.mixing == SCFT_MIX_ANDERSON && ctx->m1 > 0 &&
-         (int)ctx->hist_w.size() == ctx->m1 && ctx->gram != nullptr;
+         (int)ctx->hist_u.size() == ctx->m1 && ctx->gram != nullptr;
 }
 
 }  // namespace
@@ -308,13 +313,14 @@ int scft_save_checkpoint(scft_ctx *ctx, const char *path, int with_history) {
   const scft_params &p = ctx->p;
   CkptHeader h;
   memset(&h, 0, sizeof h);
-  memcpy(h.magic, "SCFTCKP1", 8);
-  h.version = 1;
+  memcpy(h.magic, "SCFTCKP2", 8);
+  h.version = 2;
   h.nx = p.nx; h.ny = p.ny; h.nz = p.nz; h.batch = ctx->batch;
   h.precision = p.precision; h.mixing = p.mixing; h.history = p.anderson_history;
   h.has_history = (with_history && history_kept(ctx)) ? 1 : 0;
   h.lx = p.lx; h.ly = p.ly; h.lz = p.lz; h.hAB = p.hAB; h.fA = p.fA; h.ds0 = p.ds0;
   h.and_count = ctx->and_count;
+  h.anderson_lambda = p.anderson_lambda;
   FILE *fp = fopen(path, "wb");
   if (!fp) return scft_fail(ctx, SCFT_ERR_IO, std::string("cannot write ") + path);
   int rc = fwrite(&h, sizeof h, 1, fp) == 1 ? SCFT_OK
@@ -326,7 +332,7 @@ int scft_save_checkpoint(scft_ctx *ctx, const char *path, int with_history) {
   if (rc == SCFT_OK && h.has_history) {
     const int32_t m1 = ctx->m1;
     if (fwrite(&m1, sizeof m1, 1, fp) != 1) rc = scft_fail(ctx, SCFT_ERR_IO, "checkpoint write failed");
-    for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = dev_to_file(ctx, fp, ctx->hist_w[j], 2 * BM);
+    for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = dev_to_file(ctx, fp, ctx->hist_u[j], 2 * BM);
     for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = dev_to_file(ctx, fp, ctx->hist_d[j], 2 * BM);
     if (rc == SCFT_OK) rc = dev_to_file(ctx, fp, ctx->gram, (long long)ctx->batch * m1 * m1);
   }
@@ -343,8 +349,8 @@ int scft_load_checkpoint(scft_ctx *ctx, const char *path) {
     return scft_fail(ctx, st, m);
   };
   CkptHeader h;
-  if (fread(&h, sizeof h, 1, fp) != 1 || memcmp(h.magic, "SCFTCKP1", 8) != 0 || h.version != 1)
-    return io_fail(SCFT_ERR_IO, std::string("not a checkpoint file: ") + path);
+  if (fread(&h, sizeof h, 1, fp) != 1 || memcmp(h.magic, "SCFTCKP2", 8) != 0 || h.version != 2)
+    return io_fail(SCFT_ERR_IO, std::string("not a checkpoint file of this version: ") + path);
   const scft_params &p = ctx->p;
   if (h.nx != p.nx || h.ny != p.ny || h.nz != p.nz || h.batch != ctx->batch)
     return io_fail(SCFT_ERR_INVALID_ARG, "checkpoint grid or batch differs from the context");
@@ -395,9 +401,10 @@ int scft_load_checkpoint(scft_ctx *ctx, const char *path) {
     const bool same = history_kept(ctx) && h.precision == p.precision &&
                       h.mixing == p.mixing && h.history == p.anderson_history &&
                       h.lx == p.lx && h.ly == p.ly && h.lz == p.lz && h.hAB == p.hAB &&
-                      h.fA == p.fA && h.ds0 == p.ds0;
+                      h.fA == p.fA && h.ds0 == p.ds0 &&
+                      h.anderson_lambda == p.anderson_lambda;
     if (same && m1 == ctx->m1 && fseek(fp, (long)(off_m1 + (long long)sizeof m1), SEEK_SET) == 0) {
-      for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = file_to_dev(ctx, fp, ctx->hist_w[j], 2 * BM);
+      for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = file_to_dev(ctx, fp, ctx->hist_u[j], 2 * BM);
       for (int j = 0; j < m1 && rc == SCFT_OK; ++j) rc = file_to_dev(ctx, fp, ctx->hist_d[j], 2 * BM);
       if (rc == SCFT_OK) rc = file_to_dev(ctx, fp, ctx->gram, (long long)ctx->batch * m1 * m1);
       if (rc == SCFT_OK) ctx->and_count = h.and_count;

@@ -5,14 +5,22 @@
 // Residual (phi_w's update direction before the wopt step, cuda_aid.cu:398-408):
 //   dA = hAB*phB + eta - wA - wcmp*(1-phA-phB),  dB = hAB*phA + eta - wB - wcmp*(...)
 // Anderson (Anderson 1965, in the form used for SCFT by Thompson et al. 2004 and
-// Matsen 2009): keep the last m+1 pairs (w_j, d_j) in a ring; with G_ij = <d_i, d_j>
-// (both fields, all points, FP64) and the current slot c,
+// Matsen 2009): keep the last m+1 iterations in a ring; with G_ij = <d_i, d_j>
+// (both fields, all points) and the current slot c,
 //   U_ij = G_cc - G_c,ci - G_c,cj + G_ci,cj ,  V_i = G_cc - G_c,ci   (ci = slot c-i)
 //   solve U x = V (FP64, one warp);  a_c = 1 - sum x_i, a_ci = x_i
-//   w_new = sum_j a_j (w_j + lambda d_j)
+//   w_new = sum_j a_j (w_j + lambda d_j) = sum_j a_j u_j
+// The ring holds u_j = w_j + lambda d_j (what the update reads) and d_j (what
+// the Gram row reads), each as double-float pairs (hi, lo floats, about 48
+// significant bits, dfloat.cuh): the Gram row and the update are sums of
+// products over all slots and points, which on GB300's FP64 pipe took 3x
+// their memory time; in pair arithmetic on the FP32 pipe they run at the
+// speed of their loads, and storing u instead of (w, d) halves the update's.
+// The Gram matrix, the solve and the fields stay FP64.
 // An instance whose max|d| is still above `start` (or with no history yet)
 // takes the simple step w_new = w_c + wopt d_c, decided on the device.
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "kernels.h"
 
 namespace scft {
@@ -129,14 +137,16 @@ __global__ void k_residual_mean(const double *__restrict__ partial, int nblk, lo
 // (average_value removes it every iteration), so the residual that measures
 // convergence and enters the Anderson history is d = dir - mean(dir); the
 // simple step applies the raw phi_w direction, exactly as the reference.
-// Optionally copies w and d into a history slot ([b][2][M] layout) and applies
-// the simple step in place (wopt != 0).
+// Optionally stores u = w + lam_u d and d into a history slot ([b][2][M]
+// double-float pairs), copies w to wprev ([b][2][M] FP64) and applies the
+// simple step in place (wopt != 0).
 // partial[(b*2 + {0: max|d|, 1: sum d^2})*nblk + blk]
 __global__ void k_residual(double *__restrict__ wa, double *__restrict__ wb,
                            const double *__restrict__ pha, const double *__restrict__ phb,
                            double hAB, double wcmp, double wopt, long long M,
-                           const double *__restrict__ dmean, double *__restrict__ hw,
-                           double *__restrict__ hd, double *__restrict__ partial) {
+                           const double *__restrict__ dmean, dfloat *__restrict__ hu,
+                           dfloat *__restrict__ hd, double lam_u, double *__restrict__ wprev,
+                           double *__restrict__ partial) {
   __shared__ double sh[32];
   __shared__ unsigned long long shk[32];
   const long long b = blockIdx.y, o = b * M;
@@ -152,11 +162,15 @@ __global__ void k_residual(double *__restrict__ wa, double *__restrict__ wb,
     const double ca = da - ma, cb = db - mb;
     mx = key_max(mx, key_max(abs_key(ca), abs_key(cb)));
     ss += ca * ca + cb * cb;
-    if (hw) {
-      hw[(2 * b) * M + i] = a;
-      hw[(2 * b + 1) * M + i] = c;
-      hd[(2 * b) * M + i] = ca;
-      hd[(2 * b + 1) * M + i] = cb;
+    if (hu) {
+      hu[(2 * b) * M + i] = dfloat(fma(lam_u, ca, a));
+      hu[(2 * b + 1) * M + i] = dfloat(fma(lam_u, cb, c));
+      hd[(2 * b) * M + i] = dfloat(ca);
+      hd[(2 * b + 1) * M + i] = dfloat(cb);
+    }
+    if (wprev) {
+      wprev[(2 * b) * M + i] = a;
+      wprev[(2 * b + 1) * M + i] = c;
     }
     if (wopt != 0.0) {
       wa[o + i] = a + wopt * da;   // phi_w, cuda_aid.cu:410-412
@@ -191,11 +205,26 @@ __global__ void k_residual_finalize(const double *__restrict__ partial, int nblk
   }
 }
 
+// acc += x * y in pair arithmetic, the product's error term left
+// unnormalised (it only enters the sum's low part).
+__device__ __forceinline__ void df_fma_acc(dfloat &acc, dfloat x, dfloat y) {
+  const float p = x.hi * y.hi;
+  float e = fmaf(x.hi, y.hi, -p);
+  e = fmaf(x.hi, y.lo, e);
+  e = fmaf(x.lo, y.hi, e);
+  const dfloat s = df_two_sum(acc.hi, p);
+  acc = df_fast_two_sum(s.hi, s.lo + (acc.lo + e));
+}
+__device__ __forceinline__ dfloat ld_pair(const dfloat *p) {
+  const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+  return dfloat(v.x, v.y);
+}
+
 // Gram row of slot c: <d_c, d_j> for the listed slots j (nj <= kMaxSlots).
 // partial[(b*kMaxSlots + k)*nblk + blk]
 constexpr int kMaxSlots = 33;
 struct SlotList {
-  const double *d[kMaxSlots];
+  const dfloat *d[kMaxSlots];
   int slot[kMaxSlots];
   int n;
 };
@@ -204,35 +233,33 @@ struct SlotList {
 // loads in flight per element; d_c is read once per chunk (an L2 hit while
 // it fits).
 constexpr int kChunk = 8;
-__global__ void k_gram_row(const double *__restrict__ dc, SlotList sl, long long M,
+__global__ void k_gram_row(const dfloat *__restrict__ dc, SlotList sl, long long M,
                            double *__restrict__ partial) {
   __shared__ double sh[32];
   const long long b = blockIdx.z;
   const int k0 = blockIdx.y * kChunk;
   const long long n2 = 2 * M;
-  const double *dk[kChunk];
-  double acc[kChunk];
+  const dfloat *dk[kChunk];
+  dfloat acc[kChunk];
 #pragma unroll
-  for (int kk = 0; kk < kChunk; ++kk) {
+  for (int kk = 0; kk < kChunk; ++kk)
     dk[kk] = k0 + kk < sl.n ? sl.d[k0 + kk] + b * n2 : nullptr;
-    acc[kk] = 0.0;
-  }
-  const double *x = dc + b * n2;
+  const dfloat *x = dc + b * n2;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2;
        i += (long long)gridDim.x * blockDim.x) {
-    double y[kChunk];
+    dfloat y[kChunk];
 #pragma unroll
     for (int kk = 0; kk < kChunk; ++kk)
-      if (dk[kk]) y[kk] = dk[kk][i];
-    const double xi = x[i];
+      if (dk[kk]) y[kk] = ld_pair(dk[kk] + i);
+    const dfloat xi = ld_pair(x + i);
 #pragma unroll
     for (int kk = 0; kk < kChunk; ++kk)
-      if (dk[kk]) acc[kk] += xi * y[kk];
+      if (dk[kk]) df_fma_acc(acc[kk], xi, y[kk]);
   }
 #pragma unroll
   for (int kk = 0; kk < kChunk; ++kk) {
     if (dk[kk]) {
-      const double r = blk_sum(acc[kk], sh);
+      const double r = blk_sum((double)acc[kk], sh);
       if (threadIdx.x == 0)
         partial[(b * kMaxSlots + k0 + kk) * gridDim.x + blockIdx.x] = r;
     }
@@ -258,9 +285,11 @@ __global__ void k_gram_finalize(const double *__restrict__ partial, int nblk, Sl
 
 // One warp per instance: weights a[b][slot] and the step lam_eff[b].
 // hist = number of previous slots (newest first: c-1, c-2, ...).
+// mode[b] = 1 for an Anderson step, 0 for the simple step.
 __global__ void k_anderson_solve(const double *__restrict__ G, const double *__restrict__ err,
                                  int c, int hist, int m1, double start, double lambda,
-                                 double wopt, double *__restrict__ a, double *__restrict__ lam) {
+                                 double wopt, double *__restrict__ a, double *__restrict__ lam,
+                                 double *__restrict__ mode) {
   __shared__ double U[32][33];
   __shared__ double V[32];
   const int b = blockIdx.x, lane = threadIdx.x;
@@ -273,6 +302,7 @@ __global__ void k_anderson_solve(const double *__restrict__ G, const double *__r
     if (lane == 0) {
       ab[c] = 1.0;
       lam[b] = wopt;
+      mode[b] = 0.0;
     }
     return;
   }
@@ -333,35 +363,52 @@ __global__ void k_anderson_solve(const double *__restrict__ G, const double *__r
     }
     ab[c] = 1.0 - sx;
     lam[b] = lambda;
+    mode[b] = 1.0;
   }
 }
 
-// w_new = sum_j a_j (w_j + lam d_j) over the listed slots.
-struct SlotPairs {
-  const double *w[kMaxSlots];
-  const double *d[kMaxSlots];
+// Anderson step: w_new = sum_j a_j u_j over the listed slots, in pair
+// arithmetic; simple step (mode 0): w_new = w + lam d_c in FP64 from the live
+// fields.  kUChunk slots' loads are in flight per element.
+struct SlotRing {
+  const dfloat *u[kMaxSlots];
   int idx[kMaxSlots];
   int n;
 };
-__global__ void k_anderson_update(double *__restrict__ wa, double *__restrict__ wb,
-                                  SlotPairs sp, const double *__restrict__ a,
-                                  const double *__restrict__ lam, int m1, long long M) {
-  __shared__ double s_a[kMaxSlots];   // the weights of the listed slots
+constexpr int kUChunk = 8;
+__global__ void k_anderson_update(double *__restrict__ wa, double *__restrict__ wb, SlotRing sr,
+                                  const dfloat *__restrict__ dc, const double *__restrict__ a,
+                                  const double *__restrict__ lam, const double *__restrict__ mode,
+                                  int m1, long long M) {
+  __shared__ dfloat s_a[kMaxSlots];   // the weights of the listed slots
   const long long b = blockIdx.y;
-  const double l = lam[b];
   const long long n2 = 2 * M;
-  for (int k = threadIdx.x; k < sp.n; k += blockDim.x) s_a[k] = a[b * m1 + sp.idx[k]];
-  __syncthreads();
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2;
-       i += (long long)gridDim.x * blockDim.x) {
-    double s = 0.0;
-#pragma unroll 4
-    for (int k = 0; k < sp.n; ++k) {
-      const double aj = s_a[k];
-      if (aj != 0.0) s += aj * (sp.w[k][b * n2 + i] + l * sp.d[k][b * n2 + i]);
+  const long long S = (long long)gridDim.x * blockDim.x;
+  double *wab = wa + b * M, *wbb = wb + b * M;
+  if (mode[b] == 0.0) {
+    const double l = lam[b];
+    const dfloat *d = dc + b * n2;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2; i += S) {
+      double *w = i < M ? wab + i : wbb + (i - M);
+      *w = fma(l, (double)ld_pair(d + i), *w);
     }
-    if (i < M) wa[b * M + i] = s;
-    else wb[b * M + (i - M)] = s;
+    return;
+  }
+  for (int k = threadIdx.x; k < sr.n; k += blockDim.x) s_a[k] = dfloat(a[b * m1 + sr.idx[k]]);
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2; i += S) {
+    dfloat s;
+    for (int k0 = 0; k0 < sr.n; k0 += kUChunk) {
+      dfloat y[kUChunk];
+#pragma unroll
+      for (int kk = 0; kk < kUChunk; ++kk)
+        if (k0 + kk < sr.n) y[kk] = ld_pair(sr.u[k0 + kk] + b * n2 + i);
+#pragma unroll
+      for (int kk = 0; kk < kUChunk; ++kk)
+        if (k0 + kk < sr.n) df_fma_acc(s, s_a[k0 + kk], y[kk]);
+    }
+    if (i < M) wab[i] = (double)s;
+    else wbb[i - M] = (double)s;
   }
 }
 
@@ -493,29 +540,31 @@ int anderson_max_slots() { return kMaxSlots; }
 
 cudaError_t launch_residual(double *wa, double *wb, const double *pha, const double *phb,
                             double hAB, double wcmp, double wopt, long long M, int batch,
-                            double *hw, double *hd, double *partial, int nblk, double *err,
-                            cudaStream_t st) {
+                            void *hu, void *hd, double lam_u, double *wprev, double *partial,
+                            int nblk, double *err, cudaStream_t st) {
   // err holds [b][2] results; err + 2*batch holds the [b][2] means of dA, dB
   double *dmean = err + 2 * batch;
   k_residual_sum<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, pha, phb, M, partial);
   k_residual_mean<<<batch, kThreads, 0, st>>>(partial, nblk, M, hAB, wcmp, dmean);
-  k_residual<<<dim3(nblk, batch), kThreads, 0, st>>>(wa, wb, pha, phb, hAB, wcmp, wopt, M, dmean,
-                                                    hw, hd, partial);
+  k_residual<<<dim3(nblk, batch), kThreads, 0, st>>>(
+      wa, wb, pha, phb, hAB, wcmp, wopt, M, dmean, static_cast<dfloat *>(hu),
+      static_cast<dfloat *>(hd), lam_u, wprev, partial);
   k_residual_finalize<<<batch, kThreads, 0, st>>>(partial, nblk, M, err);
   return cudaGetLastError();
 }
 
-cudaError_t launch_gram_row(const double *dc, const double *const *dj, const int *slots, int n,
+cudaError_t launch_gram_row(const void *dc, const void *const *dj, const int *slots, int n,
                             int c, int m1, long long M, int batch, double *partial, int nblk,
                             double *G, cudaStream_t st) {
+  if (n < 1 || n > kMaxSlots) return cudaErrorInvalidValue;
   SlotList sl;
   sl.n = n;
   for (int k = 0; k < n; ++k) {
-    sl.d[k] = dj[k];
+    sl.d[k] = static_cast<const dfloat *>(dj[k]);
     sl.slot[k] = slots[k];
   }
-  k_gram_row<<<dim3(nblk, (n + kChunk - 1) / kChunk, batch), kThreads, 0, st>>>(dc, sl, M,
-                                                                              partial);
+  k_gram_row<<<dim3(nblk, (n + kChunk - 1) / kChunk, batch), kThreads, 0, st>>>(
+      static_cast<const dfloat *>(dc), sl, M, partial);
   k_gram_finalize<<<dim3(n, batch), kThreads, 0, st>>>(partial, nblk, sl, c, m1, G);
   return cudaGetLastError();
 }
@@ -523,7 +572,8 @@ cudaError_t launch_gram_row(const double *dc, const double *const *dj, const int
 cudaError_t launch_anderson_solve(const double *G, const double *err, int c, int hist, int m1,
                                   double start, double lambda, double wopt, int batch,
                                   double *a, double *lam, cudaStream_t st) {
-  k_anderson_solve<<<batch, 32, 0, st>>>(G, err, c, hist, m1, start, lambda, wopt, a, lam);
+  k_anderson_solve<<<batch, 32, 0, st>>>(G, err, c, hist, m1, start, lambda, wopt, a, lam,
+                                         lam + batch);
   return cudaGetLastError();
 }
 
@@ -538,19 +588,18 @@ cudaError_t launch_remove_translation(double *wa, double *wb, const double *w0, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_anderson_update(double *wa, double *wb, const double *const *hw,
-                                   const double *const *hd, const int *idx, int n,
-                                   const double *a, const double *lam, int m1, long long M,
-                                   int batch, cudaStream_t st) {
-  SlotPairs sp;
-  sp.n = n;
+cudaError_t launch_anderson_update(double *wa, double *wb, const void *const *hu, const void *dc,
+                                   const int *idx, int n, const double *a, const double *lam,
+                                   int m1, long long M, int batch, cudaStream_t st) {
+  if (n < 1 || n > kMaxSlots) return cudaErrorInvalidValue;
+  SlotRing sr;
+  sr.n = n;
   for (int k = 0; k < n; ++k) {
-    sp.w[k] = hw[k];
-    sp.d[k] = hd[k];
-    sp.idx[k] = idx[k];
+    sr.u[k] = static_cast<const dfloat *>(hu[k]);
+    sr.idx[k] = idx[k];
   }
-  k_anderson_update<<<dim3(grid_for(2 * M), batch), kThreads, 0, st>>>(wa, wb, sp, a, lam, m1,
-                                                                       M);
+  k_anderson_update<<<dim3(grid_for(2 * M), batch), kThreads, 0, st>>>(
+      wa, wb, sr, static_cast<const dfloat *>(dc), a, lam, lam + batch, m1, M);
   return cudaGetLastError();
 }
 

@@ -118,16 +118,20 @@ cudaError_t line_filter_prepare();
 
 // ---- residual and Anderson mixing (k_anderson.cu) ----
 int anderson_max_slots();
-// residual of phi_w's update (err[b][2] = max, rms); optionally stores w, d
-// into a history slot and/or applies the simple step w += wopt*d (2 kernels)
+// residual of phi_w's update (err[b][2] = max, rms); optionally stores
+// u = w + lam_u d and d into a history slot (hu, hd: [b][2][M] double-float
+// pairs), copies w to wprev ([b][2][M] FP64) and/or applies the simple step
+// w += wopt*d (4 kernels)
 cudaError_t launch_residual(double *wa, double *wb, const double *pha, const double *phb,
                             double hAB, double wcmp, double wopt, long long M, int batch,
-                            double *hw, double *hd, double *partial, int nblk, double *err,
-                            cudaStream_t st);
-// Gram row <d_c, d_j> into the ring matrix (2 kernels)
-cudaError_t launch_gram_row(const double *dc, const double *const *dj, const int *slots, int n,
+                            void *hu, void *hd, double lam_u, double *wprev, double *partial,
+                            int nblk, double *err, cudaStream_t st);
+// Gram row <d_c, d_j> (double-float ring slots) into the FP64 ring matrix
+// (2 kernels)
+cudaError_t launch_gram_row(const void *dc, const void *const *dj, const int *slots, int n,
                             int c, int m1, long long M, int batch, double *partial, int nblk,
                             double *G, cudaStream_t st);
+// weights a[b][m1], step lam[b] and mode lam[batch + b] (1 Anderson, 0 simple)
 cudaError_t launch_anderson_solve(const double *G, const double *err, int c, int hist, int m1,
                                   double start, double lambda, double wopt, int batch,
                                   double *a, double *lam, cudaStream_t st);
@@ -137,10 +141,11 @@ cudaError_t launch_anderson_solve(const double *G, const double *err, int c, int
 cudaError_t launch_remove_translation(double *wa, double *wb, const double *w0, int nx, int ny,
                                      int nz, int batch, double *partial, int nblk,
                                      double *alpha, cudaStream_t st);
-cudaError_t launch_anderson_update(double *wa, double *wb, const double *const *hw,
-                                   const double *const *hd, const int *idx, int n,
-                                   const double *a, const double *lam, int m1, long long M,
-                                   int batch, cudaStream_t st);
+// w_new = sum_k a_k u_k over the listed ring slots (Anderson step) or
+// w + lam d_c (simple step), per instance as the solve decided
+cudaError_t launch_anderson_update(double *wa, double *wb, const void *const *hu, const void *dc,
+                                   const int *idx, int n, const double *a, const double *lam,
+                                   int m1, long long M, int batch, cudaStream_t st);
 
 // ---- field kernels (k_fields.cu) ----
 // W = exp(-w*ds2) in precision R, for batch*M points (w is FP64).

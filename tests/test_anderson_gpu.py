@@ -1,6 +1,7 @@
 """Convergence machinery on the GPU against the CPU oracle: the residual of
-the field update, Anderson mixing (FP64 Gram matrix and least squares on the
-device), convergence to |dw| < tol, and an FP32 solve polished in FP64."""
+the field update, Anderson mixing (double-float history ring, FP64 Gram
+matrix and least squares on the device), convergence to |dw| < tol, and an
+FP32 solve polished in FP64."""
 import numpy as np
 import pytest
 
@@ -56,6 +57,26 @@ def test_anderson_trajectory_matches_oracle(pkg, orc):
     scale = np.abs(ra).max()
     assert np.abs(ga - ra).max() / scale < 1e-7
     assert np.abs(gb - rb).max() / scale < 1e-7
+
+
+@pytest.mark.parametrize("iters", [12, 30])
+def test_double_float_ring_keeps_the_fp64_trajectory(pkg, orc, iters):
+    """The ring holds u = w + lambda d and d as double-float pairs (about 48
+    bits) and sums them on the FP32 pipe; an FP64 context's Anderson
+    trajectory still follows the FP64 NumPy restatement to 1e-10."""
+    wa, wb = fields(seed=1)
+    p = oparams(orc)
+    kw = dict(mixing=pkg.MIX_ANDERSON, anderson_history=8, anderson_lambda=0.5,
+              anderson_start=10.0)
+    with ctx_for(pkg, **kw) as ctx:
+        ctx.set_w(wa, wb)
+        ctx.iterate(iters)
+        ga, gb = ctx.wa, ctx.wb
+    ra, rb, *_ = orc.converge_loop(wa, wb, p, 1e-30, iters, mixing="anderson", m=8, lam=0.5,
+                                   start=10.0)
+    scale = np.abs(ra).max()
+    err = max(np.abs(ga - ra).max(), np.abs(gb - rb).max()) / scale
+    assert err < 1e-10, err
 
 
 def test_anderson_converges_to_oracle_saddle_point(pkg, orc):
