@@ -313,8 +313,8 @@ def converge_leg(pkg, dev, n=64, tol=1e-6, max_it=3000, budget_s=150.0, polishes
     FP32 propagation followed by a polish in FP64, and followed by a polish in
     double-float (FP32-pair) arithmetic.  Wall-clock seconds with a residual
     check after every iteration, inputs already on the device.  Each run then
-    continues (untimed) to 1e-7 for the correctness comparison at a tighter
-    tolerance.  pin: every path with SCFT_FLAG_PIN_TRANSLATION (Anderson
+    continues to 1e-7, timed as well: at 1e-6 each run's phi sits within about
+    1e-6 of the saddle point, so phi is compared pointwise at 1e-7 too.  pin: every path with SCFT_FLAG_PIN_TRANSLATION (Anderson
     updates without their rigid-shift component), so that the runs reach the
     same unshifted structure and phi is compared pointwise as it stands."""
     from scft_gb300 import fields as fl
@@ -341,10 +341,12 @@ def converge_leg(pkg, dev, n=64, tol=1e-6, max_it=3000, budget_s=150.0, polishes
         t64 = time.perf_counter() - t0
         r64 = float(c64.residual()[0][0])
         ref = state(c64, fe64)
-        _, fe, ok = converge_timed(c64, 1e-7, 1000, 40.0)
+        t0 = time.perf_counter()
+        it7, fe, ok = converge_timed(c64, 1e-7, 1000, 40.0)
+        t64_7 = t64 + time.perf_counter() - t0
         ref_t = state(c64, fe) if ok else None
     out["fp64"] = {"seconds": t64, "iterations": it64, "F": fe64[0, 0], "residual": r64,
-                   "converged": ok64}
+                   "converged": ok64, "seconds_to_1e-7": t64_7, "iterations_to_1e-7": it64 + it7}
 
     with pkg.Context(precision=pkg.PREC_FP32, **kw) as c32, \
             pkg.Context(precision=pkg.PREC_FP64, **kw) as p64, \
@@ -371,9 +373,13 @@ def converge_leg(pkg, dev, n=64, tol=1e-6, max_it=3000, budget_s=150.0, polishes
                    "residual": float(pol.residual()[0][0]), "converged": okp,
                    "speedup": t64 / (t32 + tp)}
             res.update(compare_to_fp64(ref, state(pol, fep)))
-            _, fe, ok = converge_timed(pol, 1e-7, 1000, 40.0)
+            t1 = time.perf_counter()
+            it7, fe, ok = converge_timed(pol, 1e-7, 1000, 40.0)
+            tp7 = t32 + tp + time.perf_counter() - t1
             if ok and ref_t is not None:
                 res["at_tol_1e-7"] = compare_to_fp64(ref_t, state(pol, fe))
+                res["at_tol_1e-7"].update(seconds=tp7, iterations_polish=itp + it7,
+                                          speedup=t64_7 / tp7)
             out[name] = res
         # errors of the FP32-propagation path against the FP64 path (the CPU
         # oracle's discretisation, matched to 1e-11) at the same fields: the
@@ -393,8 +399,13 @@ def converge_leg(pkg, dev, n=64, tol=1e-6, max_it=3000, budget_s=150.0, polishes
     ok = [nm for nm, _ in polishes if out[nm]["converged"] and out[nm]["F_abs_diff"] < 1e-7]
     best = min(ok, key=lambda k: out[k]["seconds"]) if ok else polishes[0][0]
     out.update(method=best, speedup=out[best]["speedup"], F_abs_diff=out[best]["F_abs_diff"],
+               phiA_rel_diff=out[best]["phiA_rel_diff"],
                phiA_rel_diff_shift_aligned=out[best]["phiA_rel_diff_shift_aligned"],
                Q_rel_diff=out[best]["Q_rel_diff"])
+    t7 = out[best].get("at_tol_1e-7")
+    if t7:
+        out["at_tol_1e-7"] = {"speedup": t7["speedup"], "phiA_rel_diff": t7["phiA_rel_diff"],
+                              "F_abs_diff": t7["F_abs_diff"]}
     return out
 
 

