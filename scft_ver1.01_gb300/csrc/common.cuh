@@ -20,6 +20,13 @@ template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
   r.y = a.x * b.y + a.y * b.x;
   return r;
 }
+// double-float complex product: each part one dot product of pairs
+__host__ __device__ __forceinline__ dfloat2 cmul(dfloat2 a, dfloat2 b) {
+  dfloat2 r;
+  r.x = df_dot2(a.x, b.x, a.y, -b.y);
+  r.y = df_dot2(a.x, b.y, a.y, b.x);
+  return r;
+}
 template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) {
   C r; r.x = a.x + b.x; r.y = a.y + b.y; return r;
 }

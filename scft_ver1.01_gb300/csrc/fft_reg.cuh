@@ -57,6 +57,33 @@ template <> struct real_of<float2> { typedef float type; };
 template <> struct real_of<double2> { typedef double type; };
 template <> struct real_of<dfloat2> { typedef dfloat type; };
 
+// Butterfly additions: for the double-float pair without renormalisation
+// (df_add_lazy: the codelet's products renormalise).
+template <typename C> __host__ __device__ __forceinline__ C badd(C a, C b) { return cadd(a, b); }
+template <typename C> __host__ __device__ __forceinline__ C bsub(C a, C b) { return csub(a, b); }
+template <> __host__ __device__ __forceinline__ dfloat2 badd(dfloat2 a, dfloat2 b) {
+  dfloat2 r;
+  r.x = df_add_lazy(a.x, b.x);
+  r.y = df_add_lazy(a.y, b.y);
+  return r;
+}
+template <> __host__ __device__ __forceinline__ dfloat2 bsub(dfloat2 a, dfloat2 b) {
+  dfloat2 r;
+  r.x = df_sub_lazy(a.x, b.x);
+  r.y = df_sub_lazy(a.y, b.y);
+  return r;
+}
+// v * (c + i s)
+template <typename C, typename T> __host__ __device__ __forceinline__ C rot(C v, T c, T s) {
+  return mkc<C, T>(v.x * c - v.y * s, v.x * s + v.y * c);
+}
+__host__ __device__ __forceinline__ dfloat2 rot(dfloat2 v, dfloat c, dfloat s) {
+  dfloat2 r;
+  r.x = df_dot2(v.x, c, v.y, -s);
+  r.y = df_dot2(v.x, s, v.y, c);
+  return r;
+}
+
 // v * exp(-/+ 2 pi i m / R), exact for multiples of a quarter turn.
 template <int M, int R, bool INV, typename C>
 __host__ __device__ __forceinline__ C twmul(C v) {
@@ -73,7 +100,7 @@ __host__ __device__ __forceinline__ C twmul(C v) {
   } else {
     constexpr T c = (T)cos2pi(m, R);
     constexpr T s = INV ? (T)sin2pi(m, R) : (T)-sin2pi(m, R);
-    return mkc<C, T>(v.x * c - v.y * s, v.x * s + v.y * c);
+    return rot(v, c, s);
   }
 }
 
@@ -87,35 +114,35 @@ __host__ __device__ __forceinline__ void dft(C *v) {
   if constexpr (R == 1) {
   } else if constexpr (R == 2) {
     C a = v[0], b = v[1];
-    v[0] = cadd(a, b);
-    v[1] = csub(a, b);
+    v[0] = badd(a, b);
+    v[1] = bsub(a, b);
   } else if constexpr (R == 3) {
     constexpr T s3 = (T)0.866025403784438646763723170752936183;
     C a = v[0], b = v[1], c = v[2];
-    C s = cadd(b, c), d = csub(b, c);
-    v[0] = cadd(a, s);
+    C s = badd(b, c), d = bsub(b, c);
+    v[0] = badd(a, s);
     C m = mkc<C, T>(a.x - T(0.5) * s.x, a.y - T(0.5) * s.y);
     // forward: -i*s3*d ; inverse: +i*s3*d
     C t = INV ? mkc<C, T>(-s3 * d.y, s3 * d.x) : mkc<C, T>(s3 * d.y, -s3 * d.x);
-    v[1] = cadd(m, t);
-    v[2] = csub(m, t);
+    v[1] = badd(m, t);
+    v[2] = bsub(m, t);
   } else if constexpr (R == 4) {
-    C a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-    C c = cadd(v[1], v[3]), e = csub(v[1], v[3]);
+    C a = badd(v[0], v[2]), b = bsub(v[0], v[2]);
+    C c = badd(v[1], v[3]), e = bsub(v[1], v[3]);
     C d = INV ? mkc<C, T>(-e.y, e.x) : mkc<C, T>(e.y, -e.x);
-    v[0] = cadd(a, c);
-    v[2] = csub(a, c);
-    v[1] = cadd(b, d);
-    v[3] = csub(b, d);
+    v[0] = badd(a, c);
+    v[2] = bsub(a, c);
+    v[1] = badd(b, d);
+    v[3] = bsub(b, d);
   } else if constexpr (R == 5) {
     constexpr T c1 = (T)0.309016994374947424102293417182819059;   // cos(2pi/5)
     constexpr T c2 = (T)-0.809016994374947424102293417182819059;  // cos(4pi/5)
     constexpr T s1 = (T)0.951056516295153572116439333379382143;   // sin(2pi/5)
     constexpr T s2 = (T)0.587785252292473129168705954639072769;   // sin(4pi/5)
     C a = v[0];
-    C p1 = cadd(v[1], v[4]), d1 = csub(v[1], v[4]);
-    C p2 = cadd(v[2], v[3]), d2 = csub(v[2], v[3]);
-    v[0] = cadd(a, cadd(p1, p2));
+    C p1 = badd(v[1], v[4]), d1 = bsub(v[1], v[4]);
+    C p2 = badd(v[2], v[3]), d2 = bsub(v[2], v[3]);
+    v[0] = badd(a, badd(p1, p2));
     C m1 = mkc<C, T>(a.x + c1 * p1.x + c2 * p2.x, a.y + c1 * p1.y + c2 * p2.y);
     C m2 = mkc<C, T>(a.x + c2 * p1.x + c1 * p2.x, a.y + c2 * p1.y + c1 * p2.y);
     T t1x = s1 * d1.x + s2 * d2.x, t1y = s1 * d1.y + s2 * d2.y;

@@ -62,7 +62,8 @@ template <typename C> int check_all(double tol) {
 }
 
 // Double-float arithmetic against long double: the sum within 2^-44 of
-// |a| + |b|, the product within 2^-44 of |a b| (random pairs over a wide
+// |a| + |b|, the product within 2^-44 of |a b|, the unrenormalised sums and
+// the two-product dot within 2^-44 normwise (random pairs over a wide
 // exponent range, either sign).
 int check_dfloat_ops() {
   int bad = 0;
@@ -76,6 +77,18 @@ int check_dfloat_ops() {
     worst_add = fmax(worst_add, (double)(fabsl(s - (A + B)) / (fabsl(A) + fabsl(B))));
     worst_add = fmax(worst_add, (double)(fabsl(d - (A - B)) / (fabsl(A) + fabsl(B))));
     if (A * B != 0) worst_mul = fmax(worst_mul, (double)(fabsl(p - A * B) / fabsl(A * B)));
+    // the unrenormalised butterfly additions and the two-product dot
+    // (normwise: relative to |a| + |b|, |ab| + |cd|)
+    const long double l = ld(df_add_lazy(a, b)), ls = ld(df_sub_lazy(a, b));
+    worst_add = fmax(worst_add, (double)(fabsl(l - (A + B)) / (fabsl(A) + fabsl(B))));
+    worst_add = fmax(worst_add, (double)(fabsl(ls - (A - B)) / (fabsl(A) + fabsl(B))));
+    {
+      const dfloat c(y * 0.37 + x), d(x * 1.3 - y);
+      const long double C = ld(c), D = ld(d), ref = A * B + C * D;
+      const long double nrm = fabsl(A * B) + fabsl(C * D);
+      if (nrm != 0)
+        worst_mul = fmax(worst_mul, (double)(fabsl(ld(df_dot2(a, b, c, d)) - ref) / nrm));
+    }
     // the pair is normalised: |lo| <= ulp(hi)/2
     const dfloat r = a * b;
     if (fabsf(r.lo) > 0.5f * fabsf(nextafterf(r.hi, INFINITY) - r.hi) * 1.0000001f) bad++;
