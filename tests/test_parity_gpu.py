@@ -325,6 +325,30 @@ def test_full_size_properties_128(pkg, prec, tol):
         assert np.isfinite(ctx.Q()).all()
 
 
+def test_full_size_properties_256(pkg):
+    # config 5 at full size (256^3, Ns=400, f=0.45, chiN=22, box 8.0, the
+    # lamellar/gyroid mixture), FP32: the same identities, and Q from the
+    # backward chain's last slice equal to Q from the forward chain's
+    from scft_gb300 import fields
+    n, L, ds = 256, 8.0, 0.0025
+    with pkg.Context(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, hAB=22.0, fA=0.45, ds0=ds,
+                     precision=1) as ctx:
+        assert (ctx.NsA, ctx.dNsB) == (180, 220)
+        z = np.zeros(ctx.shape)
+        ctx.set_w(z, z)
+        ctx.get_conc()
+        assert abs(ctx.Q()[0] - 1) < 2e-6
+        assert np.abs(ctx.pha - ctx.NsA * ds).max() < 2e-6
+        wa, wb = fields.mixture(n, n, n, L, L, L, 22.0, seed=0, periods=2)
+        ctx.set_w(wa, wb)
+        ctx.get_conc()
+        tot = (ctx.pha + ctx.phb).mean()
+        assert abs(tot - ds * (ctx.NsA + ctx.dNsB)) < 1e-5
+        Q = ctx.Q()[0]
+        assert abs(ctx.get_q(pkg.Q_CA, 0).mean() / Q - 1) < 2e-5
+        assert np.isfinite(ctx.pha).all() and np.isfinite(ctx.phb).all()
+
+
 def test_full_size_fp32_vs_fp64_128(pkg):
     from scft_gb300 import fields
     n, L = 128, 3.8
