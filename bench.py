@@ -320,6 +320,7 @@ def converge_leg(pkg, dev, n=64, tol=1e-6, max_it=3000, budget_s=150.0, polishes
     from scft_gb300 import fields as fl
     Lb = 3.8
     polishes = polishes or (("fp32_fp64_polish", "fp64"), ("fp32_df_polish", "df"))
+    clocks = ClockSampler(dev)   # the leg's clocks: its seconds are wall-clock
     wa, wb = fl.gyroid(n, n, n, Lb, Lb, Lb, 18.0, seed=0)
     # Anderson from the first iteration for every path (measured on this
     # config: FP64 142 iterations against 159 with simple mixing down to 1.0)
@@ -406,6 +407,7 @@ def converge_leg(pkg, dev, n=64, tol=1e-6, max_it=3000, budget_s=150.0, polishes
     if t7:
         out["at_tol_1e-7"] = {"speedup": t7["speedup"], "phiA_rel_diff": t7["phiA_rel_diff"],
                               "F_abs_diff": t7["F_abs_diff"]}
+    out["clocks"] = clocks.stop()
     return out
 
 
