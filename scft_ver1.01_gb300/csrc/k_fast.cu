@@ -51,8 +51,12 @@ template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_
 }
 
 
-// Column passes keep the Boltzmann-factor tile of their output (N rows x 64
-// floats) in shared memory after the twiddle/gain tables.
+// FP32 column passes keep the Boltzmann-factor tile of their output (N rows
+// x 64 floats) in shared memory after the twiddle/gain tables.  With 8-byte
+// reals (FP64, double-float) the tile would take 64 KB at N = 128 and leave
+// room for one CTA (8 warps) per SM; those kernels read the factor from
+// global memory (an L2 hit) in their epilogue instead, and two CTAs fit.
+template <typename T> constexpr bool kFactorTile = sizeof(T) == 4;
 template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_wtile_off() {
   return ((fast_core_smem<T, N, XP>() + (size_t)filter_table_reals<N>() * sizeof(T) + 15) / 16) *
          16;
@@ -106,7 +110,7 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
   // land while the lines are loaded and filtered (the epilogue then reads
   // shared memory instead of waiting on global loads).
   T *s_wt = reinterpret_cast<T *>(smem_raw + fast_wtile_off<T, N, XP>());
-  if constexpr (!XP) {
+  if constexpr (!XP && kFactorTile<T>) {
     if (post) {
       constexpr int CPR = 64 / EPC;   // 16-byte copies per tile row of 64 reals
       const T *wt = post + b * w_bs;
@@ -190,7 +194,7 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
     }
   } else {
     T *dst = out + b * out_bs + base;
-    if (post) {
+    if (kFactorTile<T> && post) {
       asm volatile("cp.async.wait_all;" ::: "memory");
       __syncthreads();   // every thread's tile copies are visible
     }
@@ -199,7 +203,9 @@ __global__ void __launch_bounds__(P * 32) k_fast_line(AxisPlan ap, PassSet<T> ps
       const long long off = (long long)(p + P * j) * ap.s_n;
       C r = v[j];
       if (post) {
-        const C w = reinterpret_cast<const C *>(s_wt)[(p + P * j) * 32 + lane];
+        C w;
+        if constexpr (kFactorTile<T>) w = reinterpret_cast<const C *>(s_wt)[(p + P * j) * 32 + lane];
+        else w = ldg(reinterpret_cast<const C *>(post + b * w_bs + base + off));
         r.x *= w.x;
         r.y *= w.y;
       }
@@ -527,7 +533,7 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<T> ps) {
                              reinterpret_cast<const T *>(ap.gain), threadIdx.x, NT);
   T *s_wt = reinterpret_cast<T *>(smem_raw + fast_wtile_off<T, N, false>());
   const long long tile = (long long)blockIdx.y * ap.s_outer + (long long)blockIdx.x * 64;
-  {
+  if constexpr (kFactorTile<T>) {
     const T *wt = w + b * ps.w_bs + tile;
     for (int c = threadIdx.x; c < N * CPR; c += NT) {
       const int row = c / CPR, part = c % CPR;
@@ -551,12 +557,17 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<T> ps) {
   }
   __syncthreads();   // the shared tables are complete
   auto finish_step = [&]() {
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    __syncthreads();   // every thread's tile copies are visible
+    if constexpr (kFactorTile<T>) {
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      __syncthreads();   // every thread's tile copies are visible
+    }
     T *dq = qo + b * ps.qout_bs[set] + base;
+    const T *wg = w + b * ps.w_bs + base;
     reg::static_for<0, R1>([&](auto j_) {
       constexpr int j = decltype(j_)::value;
-      const C wv = reinterpret_cast<const C *>(s_wt)[(p + P * j) * 32 + lane];
+      C wv;
+      if constexpr (kFactorTile<T>) wv = reinterpret_cast<const C *>(s_wt)[(p + P * j) * 32 + lane];
+      else wv = ldg(reinterpret_cast<const C *>(wg + (long long)(p + P * j) * ap.s_n));
       C r = v[j];
       r.x *= wv.x;
       r.y *= wv.y;
@@ -591,7 +602,7 @@ template <typename T, int N> constexpr size_t xx_wtile_off() {
   return fast_wtile_off<T, N, true>();
 }
 template <typename T, int N> constexpr size_t xx_smem() {
-  return xx_wtile_off<T, N>() + (size_t)64 * N * sizeof(T);
+  return xx_wtile_off<T, N>() + (kFactorTile<T> ? (size_t)64 * N * sizeof(T) : 0);
 }
 
 template <typename T, int N, int P>
@@ -617,8 +628,9 @@ __global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<T> ps) {
                              reinterpret_cast<const T *>(ap.gain), threadIdx.x, NT);
   const long long base = (long long)blockIdx.x * 64 * N;   // 64 consecutive rows
   T *s_wt = reinterpret_cast<T *>(smem_raw + xx_wtile_off<T, N>());
-  {
-    const T *wt = ps.post[set] + b * ps.w_bs + base;
+  const T *wg = ps.post[set] + b * ps.w_bs + base;
+  if constexpr (kFactorTile<T>) {
+    const T *wt = wg;
     for (int c = threadIdx.x; c < 64 * N / EPC; c += NT)
       asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
                        smem_addr(s_wt + EPC * c)),
@@ -651,13 +663,17 @@ __global__ void __launch_bounds__(P * 32) k_xx(AxisPlan ap, PassSet<T> ps) {
     __syncthreads();
   };
   auto finish_step = [&]() {
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    __syncthreads();   // every thread's tile copies are visible
+    if constexpr (kFactorTile<T>) {
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      __syncthreads();   // every thread's tile copies are visible
+    }
     T *dq = ps.qout[set] + b * ps.qout_bs[set] + base;
 #pragma unroll 4
     for (int i = threadIdx.x; i < 64 * N; i += NT) {
       const int o = (i / N) * PITCH + (i % N);
-      const T w = s_wt[i];
+      T w;
+      if constexpr (kFactorTile<T>) w = s_wt[i];
+      else w = ldg(wg + i);
       const T x = stg[o] * w;
       dq[i] = x;
       stg[o] = x * w;
@@ -804,7 +820,7 @@ __global__ void __launch_bounds__(256 * G, 1)
 
 template <typename T, int N, int P, bool XP> size_t fast_smem() {
   return XP ? fast_core_smem<T, N, XP>() + (size_t)filter_table_reals<N>() * sizeof(T)
-            : fast_wtile_off<T, N, XP>() + (size_t)N * 64 * sizeof(T);
+            : fast_wtile_off<T, N, XP>() + (kFactorTile<T> ? (size_t)N * 64 * sizeof(T) : 0);
 }
 
 // Host-side shape checks of the tiled launches (the sanitizer substitute):
