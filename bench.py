@@ -762,7 +762,7 @@ def run_ours(args):
                                             "to the end of the timed region",
                            warmup_iterations_run=nw),
             "wall_s_timed": wall,
-            "converge": (converge_leg(pkg, dev) if (not args.no_converge and ws == 1)
+            "converge": (converge_leg(pkg, dev, pin=True) if (not args.no_converge and ws == 1)
                          else None),
             "converge_128": (converge_leg(pkg, dev, n=N, budget_s=120.0,
                                           polishes=(("fp32_df_polish", "df"),), pin=True)
