@@ -51,12 +51,13 @@ template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_
 }
 
 
-// FP32 column passes keep the Boltzmann-factor tile of their output (N rows
-// x 64 floats) in shared memory after the twiddle/gain tables.  With 8-byte
-// reals (FP64, double-float) the tile would take 64 KB at N = 128 and leave
-// room for one CTA (8 warps) per SM; those kernels read the factor from
-// global memory (an L2 hit) in their epilogue instead, and two CTAs fit.
-template <typename T> constexpr bool kFactorTile = sizeof(T) == 4;
+// Column passes keep the Boltzmann-factor tile of their output (N rows x 64
+// reals) in shared memory after the twiddle/gain tables.  In double-float
+// the tile would take 64 KB at N = 128 and leave room for one CTA (8 warps)
+// per SM although the registers allow two; those kernels read the factor from
+// global memory (an L2 hit) in their epilogue instead.  The FP64 kernels are
+// register-bound at one CTA per SM, so they keep the prefetched tile.
+template <typename T> constexpr bool kFactorTile = !std::is_same<T, dfloat>::value;
 template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_wtile_off() {
   return ((fast_core_smem<T, N, XP>() + (size_t)filter_table_reals<N>() * sizeof(T) + 15) / 16) *
          16;
