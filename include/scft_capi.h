@@ -325,11 +325,13 @@ int scft_read_ab_txt(const char *path, scft_params *p, int *intag);
 
 /* ---- checkpoint / metrics (no reference counterpart) ---- */
 
-/* Binary FP64 checkpoint for an exact resume (the reference's pha_<i>.dat
- * keeps 6 significant digits).  Holds the parameters and wa, wb, phiA, phiB
- * of every instance; with with_history != 0 and Anderson mixing also the
- * history ring, its Gram matrix and the iteration count, so that a run
- * resumed with the same schedule repeats the uninterrupted run bit for bit. */
+/* Binary checkpoint for an exact resume (the reference's pha_<i>.dat keeps
+ * 6 significant digits).  Holds the parameters and wa, wb, phiA, phiB of
+ * every instance in FP64; with with_history != 0 and Anderson mixing also
+ * the history ring (its double-float pairs as the device holds them), its
+ * FP64 Gram matrix, the iteration count and lambda, so that a run resumed
+ * with the same schedule repeats the uninterrupted run bit for bit.  Format
+ * version 2 (files of version 1 are refused). */
 int scft_save_checkpoint(scft_ctx *ctx, const char *path, int with_history);
 /* Restore a checkpoint into a context of the same grid and batch
  * (SCFT_ERR_INVALID_ARG otherwise).  The history is restored only when the
