@@ -176,6 +176,11 @@ def reference_cuda_leg(iters=2):
 
 
 def run_reference(args):
+    """The reference arm: the reference has no CPU path (init.cpp:119-125), so
+    its algorithm runs as the CPU restatement (the oracle, scipy.fft on every
+    host thread) on this arm's own workload: one full SCF iteration of the
+    128^3 gyroid per step (average_value x2, the four marches, Q, phi, simple
+    mixing; cuda_scft.cu:167-253)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
@@ -184,29 +189,28 @@ def run_reference(args):
     ge.load_package()
     from scft_gb300 import fields as fl
     p = orc.Params(nx=N, ny=N, nz=N, lx=L, ly=L, lz=L, hAB=CHIN, fA=FA, ds0=DS)
-    wa, _ = fl.gyroid(N, N, N, L, L, L, CHIN, seed=0)
+    wa, wb = fl.gyroid(N, N, N, L, L, L, CHIN, seed=0)
     workers = os.cpu_count()
-    sample = 8   # split steps per bench step (a bounded sample of the march)
+    pts = orc.pt_steps_per_iteration(p)
     for _ in range(args.warmup):
-        orc.march_rate_cpu(p, wa, sample, workers)
-    tot, pts = 0.0, 0
+        wa, wb, *_ = orc.iteration_cpu(wa, wb, p, workers)
+    tot = 0.0
     for _ in range(args.steps):
-        dt, n = orc.march_rate_cpu(p, wa, sample, workers)
-        tot += dt
-        pts += n
-    value = pts / tot / 1e9
+        t0 = time.perf_counter()
+        wa, wb, *_ = orc.iteration_cpu(wa, wb, p, workers)
+        tot += time.perf_counter() - t0
+    value = pts * args.steps / tot / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD + " (reference arm: 8 split steps of one propagator "
-                               "per step)", "grid": [N, N, N], "Ns": 200},
+        "config": {"workload": WORKLOAD, "grid": [N, N, N], "Ns": 200, "same_config": True},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
-                         "sample": f"{sample} forward split steps of one 128^3 propagator per "
-                                   f"step; the reference has no CPU path (init.cpp:119-125), "
-                                   f"so its algorithm runs as the CPU restatement with "
-                                   f"scipy.fft on {workers} threads"},
+                         "sample": f"{args.steps} full SCF iterations at 128^3, Ns=200 (4 "
+                                   f"marches + Q + phi + simple mixing); the reference has no "
+                                   f"CPU path (init.cpp:119-125), so its algorithm runs as the "
+                                   f"CPU restatement with scipy.fft on {workers} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "reference_cuda": reference_cuda_leg() if not args.no_ref_cuda else None,
     }
