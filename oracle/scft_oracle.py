@@ -485,26 +485,6 @@ def format_free_line(gpu_index, b, it, F, fAB, fW, fS, inc):
 
 # ---------------------------------------------------- CPU baseline (timed)
 
-def march_rate_cpu(p: Params, w: np.ndarray, n_steps: int, workers: int | None = None):
-    """Timed CPU baseline of the same step (scipy.fft, pocketfft, threaded):
-    ``n_steps`` forward split steps of one propagator over ``w``.  Returns
-    (seconds, point_steps).  Used only by bench.py's CPU-baseline legs."""
-    import time
-    import scipy.fft as sfft
-    workers = workers or os.cpu_count()
-    kdz = kxyzdz_half(p)[None]
-    wdz = np.exp(-w * p.ds2)
-    q = np.ones_like(w)
-    axes = (1, 2, 3)
-    t0 = time.perf_counter()
-    for _ in range(n_steps):
-        spec = sfft.rfftn(q * wdz, axes=axes, workers=workers)
-        spec *= kdz
-        q = sfft.irfftn(spec, s=p.shape, axes=axes, workers=workers) * wdz
-    dt = time.perf_counter() - t0
-    return dt, n_steps * w.size
-
-
 def iteration_cpu(wa, wb, p: Params, workers: int | None = None):
     """One full SCF iteration with scipy.fft (same arithmetic as free_loop's
     body, threaded FFTs).  Used only by bench.py's CPU-baseline legs."""
