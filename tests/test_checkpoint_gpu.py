@@ -1,4 +1,4 @@
-"""Binary FP64 checkpoint (exact resume) and JSON-lines progress metrics.
+"""Binary checkpoint (exact resume) and JSON-lines progress metrics.
 
 A run saved after k iterations and resumed in a fresh context must repeat
 the uninterrupted run bit for bit, with simple mixing and with Anderson
@@ -73,6 +73,25 @@ def test_history_restarts_when_the_operator_differs(pkg, tmp_path):
     with pkg.Context(**ctx_kw(pkg, "fp32", "simple")) as c:
         c.load_checkpoint(path)
         assert np.array_equal(c.wb, w2)
+
+
+def test_history_restarts_when_lambda_differs(pkg, tmp_path):
+    """The ring holds u = w + lambda d, so a history saved with another lambda
+    is not reused: the resumed run equals one loaded without any history."""
+    wa, wb = start_fields()
+    with_h, without_h = tmp_path / "h.ckpt", tmp_path / "n.ckpt"
+    with pkg.Context(**ctx_kw(pkg, "fp64", "anderson")) as a:
+        a.set_w(wa, wb)
+        a.iterate(8)
+        a.save_checkpoint(with_h)
+        a.save_checkpoint(without_h, with_history=False)
+    runs = []
+    for path in (with_h, without_h):
+        with pkg.Context(**ctx_kw(pkg, "fp64", "anderson", anderson_lambda=0.4)) as b:
+            b.load_checkpoint(path)
+            b.iterate(5)
+            runs.append((b.wa, b.wb))
+    assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
 
 
 def test_checkpoint_errors(pkg, tmp_path):
