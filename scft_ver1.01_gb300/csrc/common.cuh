@@ -56,9 +56,11 @@ __device__ __forceinline__ void pdl_release() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// pdl false: an ordinary stream-ordered launch of the same kernel (its
+// griddepcontrol instructions then return at once).
 template <typename... KArgs, typename... Args>
-inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                              cudaStream_t st, Args... args) {
+inline cudaError_t launch_k(bool pdl, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                            cudaStream_t st, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
@@ -68,8 +70,13 @@ inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = pdl ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, k, args...);
+}
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args... args) {
+  return launch_k(true, k, grid, block, smem, st, args...);
 }
 
 // Warp-level sum of a double.

@@ -58,6 +58,13 @@ template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_
 // global memory (an L2 hit) in their epilogue instead.  The FP64 kernels are
 // register-bound at one CTA per SM, so they keep the prefetched tile.
 template <typename T> constexpr bool kFactorTile = !std::is_same<T, dfloat>::value;
+
+// Programmatic dependent launch for the register kernels of real type T.  The
+// double-float kernels launch without it: their early-launched CTAs (two per
+// SM, 71 KB each) wait resident for the predecessor and keep the other march
+// chain's CTAs off those SMs (measured at 128^3: 21.46 ms per SCF iteration
+// with PDL, 20.41 ms without; FP32 the other way: 4.32 against 4.47 ms).
+template <typename T> constexpr bool kPdl = !std::is_same<T, dfloat>::value;
 template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_wtile_off() {
   return ((fast_core_smem<T, N, XP>() + (size_t)filter_table_reals<N>() * sizeof(T) + 15) / 16) *
          16;
@@ -845,7 +852,7 @@ template <typename T, int N, int P, bool XP>
 cudaError_t launch_one(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
   if (!tiles_ok(ap, N, !XP, ps)) return cudaErrorInvalidValue;
   dim3 grid(ap.n_real / 64, XP ? 1 : ap.n_outer, ps.nset * ps.batch);
-  return launch_pdl(k_fast_line<T, N, P, XP>, grid, dim3(P * 32), fast_smem<T, N, P, XP>(), st,
+  return launch_k(kPdl<T>, k_fast_line<T, N, P, XP>, grid, dim3(P * 32), fast_smem<T, N, P, XP>(), st,
                     ap, ps);
 }
 
@@ -935,7 +942,7 @@ template <typename T, int N, int P>
 cudaError_t launch_xx_t(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
   if (!tiles_ok(ap, N, false, ps)) return cudaErrorInvalidValue;
   dim3 grid(ap.n_real / 64, 1, ps.nset * ps.batch);
-  return launch_pdl(k_xx<T, N, P>, grid, dim3(P * 32), xx_smem<T, N>(), st, ap, ps);
+  return launch_k(kPdl<T>, k_xx<T, N, P>, grid, dim3(P * 32), xx_smem<T, N>(), st, ap, ps);
 }
 template <typename T, int N, int P> cudaError_t prep_zz() {
   return cudaFuncSetAttribute(k_zz<T, N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -945,7 +952,7 @@ template <typename T, int N, int P>
 cudaError_t launch_zz_t(const AxisPlan &ap, const PassSet<T> &ps, cudaStream_t st) {
   if (!tiles_ok(ap, N, true, ps)) return cudaErrorInvalidValue;
   dim3 grid(ap.n_real / 64, ap.n_outer, ps.nset * ps.batch);
-  return launch_pdl(k_zz<T, N, P>, grid, dim3(P * 32), fast_smem<T, N, P, false>(), st, ap,
+  return launch_k(kPdl<T>, k_zz<T, N, P>, grid, dim3(P * 32), fast_smem<T, N, P, false>(), st, ap,
                     ps);
 }
 // 16-byte cp.async tiles and two-real lines: refuse misaligned buffers
