@@ -334,14 +334,6 @@ int run_chain_fused(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t st, i
       ps.batch = ctx->batch;
       ps.w_bs = M;
     };
-    // With PDL each fused launch lets the next one start right after its own
-    // wait, so the next launch's CTAs come up early and wait resident.  On a
-    // 64^3 grid (64-point planes and columns on both kernels) those waiting
-    // CTAs keep the other march chain off too many SMs, and the fused kernels
-    // trigger just before their final stores instead.  Measured per SCF
-    // iteration, early -> late trigger: 64^3 1.158 -> 1.075 ms; 128^3 4.327
-    // -> 4.342; 128x128x64 2.565 -> 2.987; 64x64x128 1.721 -> 1.775.
-    const int late = apx.n == 64 && apy.n == 64 && apz.n == 64;
     int cur = 0;
     // step 1 starts with x+y and the pre factor
     reset();
@@ -361,7 +353,6 @@ int run_chain_fused(scft_ctx *ctx, const Seg *segs, int nseg, cudaStream_t st, i
       ps.qout[0] = slice(it - 1);
       ps.qout_bs[0] = qbs;
       ps.post[0] = W;
-      ps.late_release = late;
       if ((it - 1) & 1) CKL(scft::launch_zz(apz, ps, st));     // step it-1 was (x+y, z)
       else CKL(scft::launch_xyxy(apx, apy, ps, st));            // step it-1 was (z, x+y)
       cur ^= 1;

@@ -65,8 +65,6 @@ template <typename T> constexpr bool kFactorTile = !std::is_same<T, dfloat>::val
 // chain's CTAs off those SMs (measured at 128^3: 21.46 ms per SCF iteration
 // with PDL, 20.41 ms without; FP32 the other way: 4.32 against 4.47 ms).
 template <typename T> constexpr bool kPdl = !std::is_same<T, dfloat>::value;
-
-
 template <typename T, int N, bool XP> __host__ __device__ constexpr size_t fast_wtile_off() {
   return ((fast_core_smem<T, N, XP>() + (size_t)filter_table_reals<N>() * sizeof(T) + 15) / 16) *
          16;
@@ -555,7 +553,7 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<T> ps) {
     asm volatile("cp.async.commit_group;" ::: "memory");
   }
   pdl_wait();   // the input is the previous pass's output
-  if (!ps.late_release) pdl_release();
+  pdl_release();
   const long long base = tile + 2 * lane;
   C v[R1];
   {
@@ -597,7 +595,6 @@ __global__ void __launch_bounds__(P * 32) k_zz(AxisPlan ap, PassSet<T> ps) {
     finish_step();
     four_step<N, P>(v, ex, s_tw, s_g, p, lane, 0, []() {});
   }
-  if (ps.late_release) pdl_release();
   T *dst = out + b * ps.out_bs[set] + base;
   reg::static_for<0, R1>([&](auto j_) {
     constexpr int j = decltype(j_)::value;
@@ -761,7 +758,7 @@ __global__ void __launch_bounds__(256 * G, 1)
                  : "memory");
   asm volatile("cp.async.commit_group;" ::: "memory");
   pdl_wait();   // the plane is the previous pass's output
-  if (!ps.late_release) pdl_release();
+  pdl_release();
   constexpr int PER = NX * NY / NT;
 #pragma unroll
   for (int k = 0; k < PER; ++k) {
@@ -822,7 +819,6 @@ __global__ void __launch_bounds__(256 * G, 1)
   __syncthreads();
   x_pass();
   __syncthreads();
-  if (ps.late_release) pdl_release();
 #pragma unroll
   for (int k = 0; k < PER; ++k) {
     const int i = threadIdx.x + k * NT;

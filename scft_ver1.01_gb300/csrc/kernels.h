@@ -59,9 +59,6 @@ template <typename R> struct PassSet {
   // propagator slice goes; `out` then receives the next step's intermediate
   R *qout[kMaxSet];
   long long qout_bs[kMaxSet];
-  // fused step pairs: let the next launch start just before the final stores
-  // instead of right after this kernel's wait (see run_chain_fused)
-  int late_release;
   // FP32 per-axis and x+y plane passes: when set, line set blockIdx.z takes
   // its buffers and gains from desc[blockIdx.z] (nset 1, batch = sets)
   const PassDesc *desc;
